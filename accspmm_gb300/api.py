@@ -1,0 +1,289 @@
+"""Host-side mirror of the reference's C++ interface over the C ABI.
+
+The reference's calls (src/mma_tf32.cu) map one to one:
+  read_from_mtx(path)              include/mmio.hpp:171   -> accspmm_read_mtx
+  CSR(coo)                         include/format.hpp:110 -> accspmm_csr_from_coo
+  METCFBit.convertFromCSR(csr)     include/format.hpp:215 -> accspmm_metcf_from_csr
+  AdpBME.CSR2AdpBME(csr, 3, 1, 2)  include/format.hpp:340 -> accspmm_adpbme_from_metcf
+  balanceStrategy(metcf)           include/utils.hpp:75   -> accspmm_balance_strategy
+  TF32Compute.compute / adpBalanceCompute (include/tf32_comp.hpp:52, :82)
+                                                          -> accspmm_spmm_tf32 / _adaptive
+Host objects come back as numpy arrays; device objects stay library-owned
+(freed by `destroy()` or garbage collection).  Dense device buffers are any
+objects with a `data_ptr()` (torch tensors) or raw integer addresses.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .capi import ADPBME, COO, CSR, METCF, call, load
+
+_NP = {capi.u32p: np.uint32, capi.u64p: np.uint64, capi.f32p: np.float32}
+
+
+def _arr(ptr, n, dtype):
+    if n == 0 or not ptr:
+        return np.zeros(0, dtype)
+    return np.ctypeslib.as_array(ptr, (n,)).copy()
+
+
+def _ptr(a, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def _addr(x) -> int:
+    if x is None:
+        return 0
+    if hasattr(x, "data_ptr"):
+        return int(x.data_ptr())
+    return int(x)
+
+
+def _stream(s) -> C.c_void_p:
+    if s is None:
+        return C.c_void_p(0)
+    if hasattr(s, "cuda_stream"):
+        return C.c_void_p(int(s.cuda_stream))
+    return C.c_void_p(int(s))
+
+
+# ---- host objects (numpy) ---------------------------------------------------
+
+def read_from_mtx(path: str):
+    """(status, coo dict) with the reference's return codes."""
+    lib = load()
+    coo = COO()
+    st = lib.accspmm_read_mtx(path.encode(), C.byref(coo))
+    if st != capi.SUCCESS:
+        return st, None
+    out = dict(rows=coo.rows, cols=coo.cols, nnz=coo.nnz, row=_arr(coo.row, coo.nnz, np.uint32),
+               col=_arr(coo.col, coo.nnz, np.uint32), data=_arr(coo.data, coo.nnz, np.float32))
+    lib.accspmm_coo_destroy(C.byref(coo))
+    return st, out
+
+
+class _Keep:
+    """Keeps numpy arrays alive while a C struct points at them."""
+
+    def __init__(self, struct, *arrays):
+        self.struct = struct
+        self.arrays = arrays
+
+
+def coo_struct(rows, cols, row, col, data) -> _Keep:
+    row = np.ascontiguousarray(row, np.uint32)
+    col = np.ascontiguousarray(col, np.uint32)
+    data = np.ascontiguousarray(data, np.float32)
+    s = COO(rows, cols, len(row), _ptr(row, C.c_uint32), _ptr(col, C.c_uint32),
+            _ptr(data, C.c_float), capi.HOST, 0)
+    return _Keep(s, row, col, data)
+
+
+def csr_struct(csr: dict) -> _Keep:
+    rp = np.ascontiguousarray(csr["row_ptr"], np.uint32)
+    ci = np.ascontiguousarray(csr["col_idx"], np.uint32)
+    d = np.ascontiguousarray(csr["data"], np.float32)
+    s = CSR(csr["rows"], csr["cols"], len(ci), _ptr(rp, C.c_uint32), _ptr(ci, C.c_uint32),
+            _ptr(d, C.c_float), capi.HOST, 0)
+    return _Keep(s, rp, ci, d)
+
+
+def metcf_struct(m: dict) -> _Keep:
+    rwo = np.ascontiguousarray(m["rwo"], np.uint32)
+    tco = np.ascontiguousarray(m["tc_offset"], np.uint32)
+    bits = np.ascontiguousarray(m["bits"], np.uint64)
+    a2b = np.ascontiguousarray(m["a2b"], np.uint32)
+    d = np.ascontiguousarray(m["data"], np.float32)
+    s = METCF(m["rows"], m["cols"], m["nnz"], len(rwo) - 1, len(bits), _ptr(rwo, C.c_uint32),
+              _ptr(tco, C.c_uint32), _ptr(bits, C.c_uint64), _ptr(a2b, C.c_uint32),
+              _ptr(d, C.c_float), capi.HOST, 0)
+    return _Keep(s, rwo, tco, bits, a2b, d)
+
+
+def csr_from_coo(rows, cols, row, col, data) -> dict:
+    k = coo_struct(rows, cols, row, col, data)
+    out = CSR()
+    call("accspmm_csr_from_coo", C.byref(k.struct), C.byref(out), None)
+    res = csr_to_numpy(out)
+    load().accspmm_csr_destroy(C.byref(out))
+    return res
+
+
+def csr_to_numpy(c: CSR) -> dict:
+    return dict(rows=c.rows, cols=c.cols, nnz=c.nnz,
+                row_ptr=_arr(c.row_ptr, c.rows + 1, np.uint32),
+                col_idx=_arr(c.col_idx, c.nnz, np.uint32), data=_arr(c.data, c.nnz, np.float32))
+
+
+def metcf_to_numpy(m: METCF) -> dict:
+    return dict(rows=m.rows, cols=m.cols, nnz=m.nnz,
+                rwo=_arr(m.row_window_offset, m.num_windows + 1, np.uint32),
+                tc_offset=_arr(m.tc_offset, m.num_tiles + 1, np.uint32),
+                bits=_arr(m.tc_local_bit, m.num_tiles, np.uint64),
+                a2b=_arr(m.sparse_a2b, 8 * m.num_tiles, np.uint32),
+                data=_arr(m.data, m.nnz, np.float32))
+
+
+def adpbme_to_numpy(a: ADPBME) -> dict:
+    return dict(rows=a.rows, cols=a.cols, nnz=a.nnz,
+                group_offset=_arr(a.group_offset, a.num_groups + 1, np.uint32),
+                tc_offset=_arr(a.tc_offset, a.num_tiles + 1, np.uint32),
+                row_indices=_arr(a.row_indices, a.num_tiles, np.uint32),
+                bits=_arr(a.tc_local_bit, a.num_tiles, np.uint64),
+                a2b=_arr(a.sparse_a2b, 8 * a.num_tiles, np.uint32),
+                data=_arr(a.data, a.nnz, np.float32))
+
+
+def metcf_from_csr(csr: dict) -> dict:
+    k = csr_struct(csr)
+    out = METCF()
+    call("accspmm_metcf_from_csr", C.byref(k.struct), C.byref(out), None)
+    res = metcf_to_numpy(out)
+    load().accspmm_metcf_destroy(C.byref(out))
+    return res
+
+
+def adpbme_from_metcf(m: dict, t_load=3, t_comp=1, t_write=2, target_num=16) -> dict:
+    k = metcf_struct(m)
+    out = ADPBME()
+    call("accspmm_adpbme_from_metcf", C.byref(k.struct), t_load, t_comp, t_write, target_num,
+         C.byref(out), None)
+    res = adpbme_to_numpy(out)
+    load().accspmm_adpbme_destroy(C.byref(out))
+    return res
+
+
+def balance_strategy(m: dict) -> int:
+    k = metcf_struct(m)
+    flag = C.c_int(-1)
+    call("accspmm_balance_strategy", C.byref(k.struct), C.byref(flag), None)
+    return flag.value
+
+
+# ---- device objects -------------------------------------------------------------
+
+class DeviceObject:
+    """A library-owned device structure, destroyed when collected."""
+
+    _destroy = None
+
+    def __init__(self, struct):
+        self.struct = struct
+
+    def destroy(self):
+        if self.struct is not None and self.struct.owned:
+            getattr(load(), self._destroy)(C.byref(self.struct))
+        self.struct = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    @property
+    def ref(self):
+        return C.byref(self.struct)
+
+
+class DeviceCOO(DeviceObject):
+    _destroy = "accspmm_coo_destroy"
+
+
+class DeviceCSR(DeviceObject):
+    _destroy = "accspmm_csr_destroy"
+
+    @classmethod
+    def upload(cls, csr: dict, stream=None) -> "DeviceCSR":
+        k = csr_struct(csr)
+        out = CSR()
+        call("accspmm_csr_copy", C.byref(k.struct), capi.DEVICE, C.byref(out), _stream(stream))
+        _sync(stream)
+        return cls(out)
+
+
+class DeviceMETCF(DeviceObject):
+    _destroy = "accspmm_metcf_destroy"
+
+    @classmethod
+    def upload(cls, m: dict, stream=None) -> "DeviceMETCF":
+        k = metcf_struct(m)
+        out = METCF()
+        call("accspmm_metcf_copy", C.byref(k.struct), capi.DEVICE, C.byref(out), _stream(stream))
+        _sync(stream)
+        return cls(out)
+
+    @classmethod
+    def from_csr(cls, dcsr: DeviceCSR, stream=None) -> "DeviceMETCF":
+        out = METCF()
+        call("accspmm_metcf_from_csr", dcsr.ref, C.byref(out), _stream(stream))
+        return cls(out)
+
+    def to_numpy(self, stream=None) -> dict:
+        h = METCF()
+        call("accspmm_metcf_copy", self.ref, capi.HOST, C.byref(h), _stream(stream))
+        res = metcf_to_numpy(h)
+        load().accspmm_metcf_destroy(C.byref(h))
+        return res
+
+    @property
+    def c_rows(self) -> int:
+        return 8 * self.struct.num_windows
+
+    def balance_strategy(self, stream=None) -> int:
+        flag = C.c_int(-1)
+        call("accspmm_balance_strategy", self.ref, C.byref(flag), _stream(stream))
+        return flag.value
+
+    def adpbme(self, t_load=3, t_comp=1, t_write=2, target_num=16, stream=None) -> "DeviceADPBME":
+        out = ADPBME()
+        call("accspmm_adpbme_from_metcf", self.ref, t_load, t_comp, t_write, target_num,
+             C.byref(out), _stream(stream))
+        return DeviceADPBME(out)
+
+    def spmm(self, B, C_out, K: int, precision: int = capi.PREC_TF32, stream=None) -> None:
+        call("accspmm_spmm_tf32", self.ref, C.c_void_p(_addr(B)), C.c_void_p(_addr(C_out)), K,
+             precision, _stream(stream))
+
+
+class DeviceADPBME(DeviceObject):
+    _destroy = "accspmm_adpbme_destroy"
+
+    def to_numpy(self, stream=None) -> dict:
+        h = ADPBME()
+        call("accspmm_adpbme_copy", self.ref, capi.HOST, C.byref(h), _stream(stream))
+        res = adpbme_to_numpy(h)
+        load().accspmm_adpbme_destroy(C.byref(h))
+        return res
+
+    def c_rows(self, stream=None) -> int:
+        v = C.c_uint32(0)
+        call("accspmm_adaptive_c_rows", self.ref, C.byref(v), _stream(stream))
+        return v.value
+
+    def spmm(self, B, C_out, c_rows: int, K: int, precision: int = capi.PREC_TF32,
+             stream=None) -> None:
+        call("accspmm_spmm_adaptive", self.ref, C.c_void_p(_addr(B)), C.c_void_p(_addr(C_out)),
+             c_rows, K, precision, _stream(stream))
+
+
+def time_spmm(metcf: DeviceMETCF | None, adp: DeviceADPBME | None, B, C_out, c_rows: int, K: int,
+              precision=capi.PREC_TF32, warmup=10, exe=10, stream=None) -> float:
+    """TF32Compute's timing loop (include/tf32_comp.hpp:33-46): average ms."""
+    ms = C.c_float(0)
+    call("accspmm_time_spmm", metcf.ref if metcf else None, adp.ref if adp else None,
+         C.c_void_p(_addr(B)), C.c_void_p(_addr(C_out)), c_rows, K, precision, warmup, exe,
+         C.byref(ms), _stream(stream))
+    return ms.value
+
+
+def _sync(stream):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            (stream or torch.cuda.current_stream()).synchronize()
+    except ImportError:
+        pass

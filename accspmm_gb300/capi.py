@@ -1,0 +1,131 @@
+"""ctypes declarations of include/accspmm.h (libaccspmm.so).
+
+Loading fails loudly when the library has not been built: there is no Python
+or CPU fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+LIB_PATH = os.path.join(PKG, "libaccspmm.so")
+HEADER = os.path.join(ROOT, "include", "accspmm.h")
+
+u32 = C.c_uint32
+i32 = C.c_int32
+u32p = C.POINTER(C.c_uint32)
+u64p = C.POINTER(C.c_uint64)
+f32p = C.POINTER(C.c_float)
+vp = C.c_void_p
+
+SUCCESS = 0
+ERROR_READ_MTX = 3
+ERROR_ARGS = 4
+MM_LOADING_FILE_ERROR = -1
+MM_READ_BANNER_ERROR = -2
+ERROR_INVALID_VALUE = 30
+ERROR_ALLOC = 31
+ERROR_CUDA = 32
+ERROR_UNSUPPORTED = 33
+ERROR_OVERFLOW = 34
+ERROR_TIMEOUT = 35
+ERROR_ADMISSION = 36
+ERROR_CANCELLED = 37
+PREC_TF32 = 0
+PREC_3XTF32 = 1
+HOST = 0
+DEVICE = 1
+
+
+class COO(C.Structure):
+    _fields_ = [("rows", u32), ("cols", u32), ("nnz", u32), ("row", u32p), ("col", u32p),
+                ("data", f32p), ("space", i32), ("owned", i32)]
+
+
+class CSR(C.Structure):
+    _fields_ = [("rows", u32), ("cols", u32), ("nnz", u32), ("row_ptr", u32p),
+                ("col_idx", u32p), ("data", f32p), ("space", i32), ("owned", i32)]
+
+
+class METCF(C.Structure):
+    _fields_ = [("rows", u32), ("cols", u32), ("nnz", u32), ("num_windows", u32),
+                ("num_tiles", u32), ("row_window_offset", u32p), ("tc_offset", u32p),
+                ("tc_local_bit", u64p), ("sparse_a2b", u32p), ("data", f32p),
+                ("space", i32), ("owned", i32)]
+
+
+class ADPBME(C.Structure):
+    _fields_ = [("rows", u32), ("cols", u32), ("nnz", u32), ("num_tiles", u32),
+                ("num_groups", u32), ("group_offset", u32p), ("tc_offset", u32p),
+                ("row_indices", u32p), ("tc_local_bit", u64p), ("sparse_a2b", u32p),
+                ("data", f32p), ("space", i32), ("owned", i32)]
+
+
+_SIGS = {
+    "accspmm_version": ([], C.c_char_p),
+    "accspmm_last_error": ([], C.c_char_p),
+    "accspmm_read_mtx": ([C.c_char_p, C.POINTER(COO)], C.c_int),
+    "accspmm_csr_from_coo": ([C.POINTER(COO), C.POINTER(CSR), vp], C.c_int),
+    "accspmm_metcf_from_csr": ([C.POINTER(CSR), C.POINTER(METCF), vp], C.c_int),
+    "accspmm_adpbme_from_metcf": ([C.POINTER(METCF), u32, u32, u32, u32, C.POINTER(ADPBME), vp],
+                                  C.c_int),
+    "accspmm_balance_strategy": ([C.POINTER(METCF), C.POINTER(C.c_int), vp], C.c_int),
+    "accspmm_adaptive_c_rows": ([C.POINTER(ADPBME), u32p, vp], C.c_int),
+    "accspmm_metcf_copy": ([C.POINTER(METCF), i32, C.POINTER(METCF), vp], C.c_int),
+    "accspmm_csr_copy": ([C.POINTER(CSR), i32, C.POINTER(CSR), vp], C.c_int),
+    "accspmm_coo_copy": ([C.POINTER(COO), i32, C.POINTER(COO), vp], C.c_int),
+    "accspmm_adpbme_copy": ([C.POINTER(ADPBME), i32, C.POINTER(ADPBME), vp], C.c_int),
+    "accspmm_coo_destroy": ([C.POINTER(COO)], None),
+    "accspmm_csr_destroy": ([C.POINTER(CSR)], None),
+    "accspmm_metcf_destroy": ([C.POINTER(METCF)], None),
+    "accspmm_adpbme_destroy": ([C.POINTER(ADPBME)], None),
+    "accspmm_spmm_tf32": ([C.POINTER(METCF), vp, vp, u32, i32, vp], C.c_int),
+    "accspmm_spmm_adaptive": ([C.POINTER(ADPBME), vp, vp, u32, u32, i32, vp], C.c_int),
+    "accspmm_time_spmm": ([C.POINTER(METCF), C.POINTER(ADPBME), vp, vp, u32, u32, i32, i32, i32,
+                           f32p, vp], C.c_int),
+}
+
+_LIB = None
+
+
+class AccSpmmError(RuntimeError):
+    def __init__(self, fn: str, status: int, msg: str):
+        super().__init__(f"{fn} returned {status}: {msg}")
+        self.status = status
+
+
+def header_functions() -> list:
+    """Names of the functions declared in include/accspmm.h."""
+    with open(HEADER) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(accspmm_\w+)\s*\(", text)))
+
+
+def load():
+    """Loads libaccspmm.so; raises if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with "
+                           "`python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(LIB_PATH)
+    for name, (args, res) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _LIB = lib
+    return lib
+
+
+def check(fn: str, status: int) -> None:
+    if status != SUCCESS:
+        raise AccSpmmError(fn, status, load().accspmm_last_error().decode())
+
+
+def call(name: str, *args) -> None:
+    check(name, getattr(load(), name)(*args))

@@ -1,0 +1,28 @@
+// host_formats.hpp -- host-side builders (host_formats.cpp).
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "accspmm.h"
+
+namespace accspmm {
+
+int read_mtx_host(const char* path, accspmm_coo_t* coo);
+int csr_from_coo_host(const accspmm_coo_t* coo, accspmm_csr_t* csr);
+int metcf_from_csr_host(const accspmm_csr_t* csr, accspmm_metcf_t* out);
+std::vector<uint32_t> adp_groups_host(uint32_t W, const uint32_t* rwo, uint32_t t_load,
+                                      uint32_t t_comp, uint32_t t_write, uint32_t target_num);
+int adpbme_from_metcf_host(const accspmm_metcf_t* m, uint32_t t_load, uint32_t t_comp,
+                           uint32_t t_write, uint32_t target_num, accspmm_adpbme_t* a);
+int balance_strategy_host(const uint32_t* rwo, uint32_t W, uint32_t T);
+
+// device builders (metcf_device.cu)
+int csr_from_coo_device(const accspmm_coo_t* coo, accspmm_csr_t* csr, void* stream);
+int metcf_from_csr_device(const accspmm_csr_t* csr, accspmm_metcf_t* out, void* stream);
+int adpbme_from_metcf_device(const accspmm_metcf_t* m, uint32_t t_load, uint32_t t_comp,
+                             uint32_t t_write, uint32_t target_num, accspmm_adpbme_t* a,
+                             void* stream);
+int balance_strategy_device(const accspmm_metcf_t* m, int* adaptive, void* stream);
+
+}  // namespace accspmm

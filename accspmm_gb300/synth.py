@@ -39,7 +39,12 @@ def powerlaw_degrees(n: int, alpha: float, mean: float, d_max: int,
 
 def _dedupe_sorted(rows: np.ndarray, cols: np.ndarray, n_cols: int):
     key = rows.astype(np.int64) * np.int64(n_cols) + cols.astype(np.int64)
-    key = np.unique(key)
+    key.sort()
+    keep = np.empty(key.size, dtype=bool)
+    if key.size:
+        keep[0] = True
+        np.not_equal(key[1:], key[:-1], out=keep[1:])
+    key = key[keep]
     return (key // n_cols).astype(np.uint32), (key % n_cols).astype(np.uint32)
 
 

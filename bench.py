@@ -1,0 +1,396 @@
+#!/usr/bin/env python
+"""METCF SpMM throughput on the 1M-row power-law workload (one JSON line).
+
+Workload: N = 1,048,576 rows, power-law degrees (Zipf alpha 2.1, mean 32, max
+4,096), half the neighbours within +-1,024 of the row, half uniform, values
+uniform[0, 1); B is N x K float32 uniform[-1, 1), K = 128 by default.  Seeded
+synthetic data stands in for the reference's missing dataset.  One step is one
+SpMM over the whole matrix through the C ABI, on the path the reference's
+driver would pick (balanceStrategy -> adaptive or plain).  B (512 MB at
+K = 128) and the METCF arrays are larger than the 129 MB L2, so no L2 flush
+is done between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU CSR SpMM (the oracle's OpenMP port, the
+reference has no CPU SpMM of its own) on all host cores for the same metric.
+Under torchrun with more than one rank, every rank runs an independent replica
+on its own GPU (the workload does not shard in this build); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SpMM GFLOP/s (2*nnz*K)"
+UNIT = "GFLOP/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--k", type=int, default=128)
+    p.add_argument("--n", type=int, default=1 << 20)
+    p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--precision", default="tf32", choices=["tf32", "3xtf32"])
+    p.add_argument("--no-sweep", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-host-build", action="store_true")
+    return p.parse_args()
+
+
+def workload(n: int, seed: int):
+    from accspmm_gb300 import synth
+    cache = f"/tmp/accspmm_powerlaw_local_{n}_{seed}.npz"
+    if os.path.exists(cache):
+        z = np.load(cache)
+        return z["rp"], z["ci"], z["v"]
+    rp, ci, v = synth.powerlaw_local(n=n, seed=seed)
+    try:
+        np.savez(cache, rp=rp, ci=ci, v=v)
+    except OSError:
+        pass
+    return rp, ci, v
+
+
+def workload_name(n, k):
+    return (f"powerlaw_local N={n} mean_deg=32 zipf=2.1 max_deg=4096 local=50%/+-1024 "
+            f"B=N x {k} fp32 uniform[-1,1)")
+
+
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(nnz, T, W, cols, K, G=None):
+    """Compulsory traffic of one SpMM: values, bitmaps, tcOffset, sparseA2B,
+    rowWindowOffset, B read once, C written once (+ AdpBME row indices and
+    group offsets on the adaptive path)."""
+    b = 4 * nnz + 8 * T + 4 * (T + 1) + 32 * T + 4 * (W + 1) + 4 * cols * K + 4 * 8 * W * K
+    if G is not None:
+        b += 4 * T + 4 * (G + 1)
+    return b
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def measured_traffic(K):
+    """DRAM bytes per launch of the SpMM kernel from the committed ncu summary
+    (profiles/spmm_window_kernel_powerlaw_local.md), if one exists for K."""
+    path = os.path.join(ROOT, "profiles", "spmm_window_kernel_powerlaw_local.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith(f"traffic_bytes_per_launch K={K}:"):
+                    return int(line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(rp, ci, v, B, budget_s=8.0):
+    from oracle import oracle
+    threads = oracle.omp_max_threads()
+    C = np.zeros((len(rp) - 1, B.shape[1]), np.float32)
+    oracle.spmm_csr_f32_omp(rp, ci, v, B, C, threads=threads)  # warm
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        oracle.spmm_csr_f32_omp(rp, ci, v, B, C, threads=threads)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or reps >= 10:
+            break
+    gf = 2.0 * len(ci) * B.shape[1] * reps / el / 1e9
+    return {"value": round(gf, 2), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"full matrix ({len(ci)} nnz, K={B.shape[1]}), {reps} reps, "
+                      f"FP32 CSR SpMM, OpenMP over rows"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    rp, ci, v = workload(args.n, args.seed)
+    B = np.random.default_rng(args.seed + 7).uniform(-1, 1, (args.n, args.k)).astype(np.float32)
+    from oracle import oracle
+    threads = oracle.omp_max_threads()
+    C = np.zeros((args.n, args.k), np.float32)
+    for _ in range(max(args.warmup, 1)):
+        oracle.spmm_csr_f32_omp(rp, ci, v, B, C, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.spmm_csr_f32_omp(rp, ci, v, B, C, threads=threads)
+    el = time.perf_counter() - t0
+    ms = el / args.steps * 1e3
+    gf = 2.0 * len(ci) * args.k / (ms * 1e-3) / 1e9
+    out = {
+        "metric": METRIC, "value": round(gf, 2), "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": workload_name(args.n, args.k), "n_rows": args.n, "nnz": int(len(ci)),
+                   "K": args.k, "path": "CPU CSR SpMM (oracle port; the reference has no CPU SpMM)"},
+        "cpu_baseline": {"value": round(gf, 2), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"full matrix per step, {args.steps} steps"},
+        "e2e": {"value": round(gf, 2), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from accspmm_gb300 import api, capi
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    prec = capi.PREC_3XTF32 if args.precision == "3xtf32" else capi.PREC_TF32
+    K = args.k
+
+    rp, ci, vals = workload(args.n, args.seed)
+    n, nnz = args.n, int(len(ci))
+    csr = dict(rows=n, cols=n, nnz=nnz, row_ptr=rp, col_idx=ci, data=vals)
+    stream = torch.cuda.current_stream()
+
+    # METCF on the GPU (timed once, as information)
+    dcsr = api.DeviceCSR.upload(csr, stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    m = api.DeviceMETCF.from_csr(dcsr, stream)
+    torch.cuda.synchronize()
+    device_build_ms = (time.perf_counter() - t0) * 1e3
+    dcsr.destroy()
+    host_build_ms = None
+    if not args.no_host_build and rank == 0:
+        t0 = time.perf_counter()
+        api.metcf_from_csr(csr)
+        host_build_ms = (time.perf_counter() - t0) * 1e3
+    T, W = m.struct.num_tiles, m.struct.num_windows
+    adaptive = m.balance_strategy(stream)
+    adp, G = None, None
+    if adaptive:
+        adp = m.adpbme(stream=stream)
+        G = adp.struct.num_groups
+        c_rows = adp.c_rows(stream)
+    else:
+        c_rows = m.c_rows
+    gen = torch.Generator(device=dev).manual_seed(args.seed)
+    B = torch.rand((n, K), device=dev, generator=gen) * 2 - 1
+    C = torch.empty((c_rows, K), device=dev)
+
+    def step(Bt, Ct):
+        if adaptive:
+            adp.spmm(Bt, Ct, c_rows, K, prec, stream)
+        else:
+            m.spmm(Bt, Ct, K, prec, stream)
+
+    launches_per_step = 2 if adaptive else 1
+    for _ in range(max(args.warmup, 3)):
+        step(B, C)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step(B, C)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    flops = 2.0 * nnz * K
+    value = flops * world / (ms * 1e-3) / 1e9
+
+    # dominant kernel alone: the plain entry point is exactly one launch of it
+    for _ in range(3):
+        m.spmm(B, C, K, prec, stream)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    reps = 10
+    for _ in range(reps):
+        m.spmm(B, C, K, prec, stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    kms = e0.elapsed_time(e1) / reps
+    abytes = algorithmic_bytes(nnz, T, W, n, K)
+    achieved = abytes / (kms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = measured_traffic(K)
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic,
+                "peak_source": f"{peak_kind} hbm_gbs", "kernel": "spmm_window_kernel",
+                "kernel_ms": round(kms, 4), "algorithmic_bytes": int(abytes)}
+    if traffic:
+        roofline["dram_gbs"] = round(traffic / (kms * 1e-3) / 1e9, 1)
+
+    # end to end through the C ABI with host buffers: B host->device, SpMM,
+    # C device->host, every step
+    Bh = torch.empty((n, K), dtype=torch.float32, pin_memory=True)
+    Bh.copy_(B.cpu())
+    Ch = torch.empty((c_rows, K), dtype=torch.float32, pin_memory=True)
+    Bd = torch.empty_like(B)
+    e2e_steps = max(3, min(args.steps, 10))
+    for _ in range(2):
+        Bd.copy_(Bh, non_blocking=True)
+        step(Bd, C)
+        Ch.copy_(C, non_blocking=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        Bd.copy_(Bh, non_blocking=True)
+        step(Bd, C)
+        Ch.copy_(C, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    e2e = {"value": round(flops * world / (e2e_ms * 1e-3) / 1e9, 2), "unit": UNIT,
+           "h2d_bytes_per_step": int(Bh.numel() * 4), "d2h_bytes_per_step": int(Ch.numel() * 4),
+           "ms_per_step": round(e2e_ms, 3)}
+
+    sweep = {}
+    if not args.no_sweep and rank == 0:
+        for kk in (32, 64, 128, 256):
+            Bk = torch.rand((n, kk), device=dev, generator=gen) * 2 - 1
+            Ck = torch.empty((c_rows, kk), device=dev)
+            for _ in range(3):
+                (adp.spmm(Bk, Ck, c_rows, kk, prec, stream) if adaptive else m.spmm(Bk, Ck, kk, prec, stream))
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(10):
+                (adp.spmm(Bk, Ck, c_rows, kk, prec, stream) if adaptive else m.spmm(Bk, Ck, kk, prec, stream))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            kt = e0.elapsed_time(e1) / 10
+            sweep[str(kk)] = {"ms": round(kt, 4), "gflops": round(2.0 * nnz * kk / (kt * 1e-3) / 1e9, 1),
+                              "gbs_algorithmic": round(algorithmic_bytes(nnz, T, W, n, kk) / (kt * 1e-3) / 1e9, 1)}
+            del Bk, Ck
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        Bnp = B[:, :].cpu().numpy()
+        cpu = cpu_baseline(rp, ci, vals, Bnp)
+    out = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": args.precision, "data": "synthetic",
+        "config": {"workload": workload_name(n, K), "n_rows": n, "nnz": nnz, "K": K,
+                   "tiles": int(T), "windows": int(W), "groups": G,
+                   "path": "adaptive" if adaptive else "plain",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "no flush: B (N*K*4 bytes) and METCF exceed the 129 MB L2",
+                   "metcf_build_ms": {"device": round(device_build_ms, 1),
+                                      "host": round(host_build_ms, 1) if host_build_ms else None},
+                   "seed": args.seed},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": args.steps * launches_per_step,
+        "clocks": clk.summary(),
+        "k_sweep": sweep,
+    }
+    print(json.dumps(out))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

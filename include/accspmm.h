@@ -1,0 +1,220 @@
+/*
+ * accspmm.h -- C ABI of the GB300 METCF SpMM library (libaccspmm.so).
+ *
+ * Drop-in boundary for the AccSpMM path: Matrix Market load -> CSR -> METCF
+ * (8x8 row-window tiles with 64-bit occupancy bitmaps) -> load-balance choice
+ * -> AdpBME grouping -> TF32 tensor-core SpMM C = A * B.  Each entry point
+ * names the reference interface it replaces (paths relative to the AccSpMM
+ * source tree).  The reference has no library ABI; its interface is the set of
+ * header-only C++ calls made by src/mma_tf32.cu, and this header restates each
+ * of them with plain pointers and sizes.
+ *
+ * Conventions
+ *  - Every function returns an int status (ACCSPMM_SUCCESS == 0).  Codes that
+ *    exist in include/common.hpp:71-95 keep their numeric values.  Errors are
+ *    returned, never printed and ignored (the reference prints CUDA errors
+ *    and continues, include/utils.hpp:6-22); accspmm_last_error() gives the
+ *    message of the calling thread's last failure.
+ *  - Index and offset arrays are uint32 like the reference's `vint`;
+ *    products with the feature width are computed in 64-bit.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ *    stream).  Device work is enqueued on it; functions that must return a
+ *    host value (sizes, flags) synchronise that stream.
+ *  - Objects whose `space` is ACCSPMM_DEVICE hold device pointers.  Objects
+ *    filled by the library own their arrays; release them with the matching
+ *    *_destroy call.  Objects a caller fills by hand are never freed by the
+ *    library.
+ *  - Dense matrices are row-major float32: B has `cols` rows and K columns,
+ *    C has 8 * num_windows rows (plain path) or `c_rows` rows (adaptive path)
+ *    and K columns; K must be a positive multiple of 4 and B, C 16-byte
+ *    aligned.
+ */
+#ifndef ACCSPMM_H
+#define ACCSPMM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    ACCSPMM_SUCCESS = 0,              /* SUCCESS            common.hpp:83 */
+    ACCSPMM_ERROR_NOT_MATCH = 1,      /* ERROR_NOT_MATCH    common.hpp:72 */
+    ACCSPMM_ERROR_OPEN_FILE = 2,      /* ERROR_OPEN_FILE    common.hpp:73 */
+    ACCSPMM_ERROR_READ_MTX = 3,       /* ERROR_READ_MTX     common.hpp:74 */
+    ACCSPMM_ERROR_ARGS = 4,           /* ERROR_ARGS         common.hpp:75 */
+    ACCSPMM_MM_LOADING_FILE_ERROR = -1, /* common.hpp:84 */
+    ACCSPMM_MM_READ_BANNER_ERROR = -2,  /* common.hpp:85 */
+    ACCSPMM_RET_ERROR = -4,             /* common.hpp:86 */
+    ACCSPMM_MM_PREMATURE_EOF = 12,      /* common.hpp:90 */
+    ACCSPMM_MM_UNSUPPORTED_TYPE = 15,   /* common.hpp:93 */
+    /* no counterpart in the reference */
+    ACCSPMM_ERROR_INVALID_VALUE = 30,
+    ACCSPMM_ERROR_ALLOC = 31,
+    ACCSPMM_ERROR_CUDA = 32,
+    ACCSPMM_ERROR_UNSUPPORTED = 33,
+    ACCSPMM_ERROR_OVERFLOW = 34,
+    ACCSPMM_ERROR_TIMEOUT = 35,
+    ACCSPMM_ERROR_ADMISSION = 36,
+    ACCSPMM_ERROR_CANCELLED = 37
+};
+
+/* arithmetic of the SpMM */
+enum {
+    ACCSPMM_PREC_TF32 = 0,   /* both operands rounded to TF32 (cvt.rna), FP32 accumulate */
+    ACCSPMM_PREC_3XTF32 = 1  /* hi/lo TF32 splits of A and B, three MMAs, FP32 accumulate */
+};
+
+/* memory space of an object's arrays */
+enum { ACCSPMM_HOST = 0, ACCSPMM_DEVICE = 1 };
+
+/* ---- formats ----------------------------------------------------------- */
+/* COO<T>, include/format.hpp:33-94 (0-based indices). */
+typedef struct accspmm_coo {
+    uint32_t rows, cols, nnz;
+    uint32_t* row;
+    uint32_t* col;
+    float* data;
+    int32_t space;
+    int32_t owned;
+} accspmm_coo_t;
+
+/* CSR<T>, include/format.hpp:96-169. */
+typedef struct accspmm_csr {
+    uint32_t rows, cols, nnz;
+    uint32_t* row_ptr;   /* [rows + 1] */
+    uint32_t* col_idx;   /* [nnz] */
+    float* data;         /* [nnz] */
+    int32_t space;
+    int32_t owned;
+} accspmm_csr_t;
+
+/* METCFBit<T>, include/format.hpp:202-274.  W = ceil(rows / 8) row windows,
+ * T tiles of 8 rows x 8 distinct columns. */
+typedef struct accspmm_metcf {
+    uint32_t rows, cols, nnz;
+    uint32_t num_windows;          /* W */
+    uint32_t num_tiles;            /* T */
+    uint32_t* row_window_offset;   /* [W + 1] rowWindowOffset */
+    uint32_t* tc_offset;           /* [T + 1] tcOffset */
+    uint64_t* tc_local_bit;        /* [T]     tcLocalBit, bit (r%8)*8 + c%8 */
+    uint32_t* sparse_a2b;          /* [8T]    sparseA2B, UINT32_MAX = padding */
+    float* data;                   /* [nnz]   values, tile by tile */
+    int32_t space;
+    int32_t owned;
+} accspmm_metcf_t;
+
+/* AdpBME<T>, include/format.hpp:327-429. */
+typedef struct accspmm_adpbme {
+    uint32_t rows, cols, nnz;
+    uint32_t num_tiles;            /* T */
+    uint32_t num_groups;           /* G */
+    uint32_t* group_offset;        /* [G + 1] groupOffset */
+    uint32_t* tc_offset;           /* [T + 1] */
+    uint32_t* row_indices;         /* [T]     first row of each tile's window */
+    uint64_t* tc_local_bit;        /* [T] */
+    uint32_t* sparse_a2b;          /* [8T] */
+    float* data;                   /* [nnz] */
+    int32_t space;
+    int32_t owned;
+} accspmm_adpbme_t;
+
+/* ---- library ----------------------------------------------------------- */
+const char* accspmm_version(void);
+/* Message of the calling thread's most recent failing call ("" if none). */
+const char* accspmm_last_error(void);
+
+/* ---- loading and conversion (host) -------------------------------------- */
+/* read_from_mtx<float>, include/mmio.hpp:171-210 (with mm_read_banner :24,
+ * mm_read_mtx_crd_size :74, handle_coo :106).  Same return codes: 0,
+ * MM_LOADING_FILE_ERROR, MM_READ_BANNER_ERROR, ERROR_READ_MTX.  Symmetric and
+ * Hermitian files are expanded (nnz' = 2 nnz - diag) in the reference's
+ * order; pattern -> 1.0; complex keeps the real part.  Unlike the reference,
+ * integer values are parsed as integers, and a truncated or out-of-range
+ * entry list returns ERROR_READ_MTX instead of undefined data.  The body is
+ * parsed on all host threads. */
+int accspmm_read_mtx(const char* path, accspmm_coo_t* coo);
+
+/* CSR<T>::CSR(const COO<T>*), include/format.hpp:110-142: stable counting
+ * sort by row.  Host -> host, or device -> device when coo->space is
+ * ACCSPMM_DEVICE (stream-ordered). */
+int accspmm_csr_from_coo(const accspmm_coo_t* coo, accspmm_csr_t* csr,
+                         void* stream);
+
+/* METCFBit<T>::convertFromCSR, include/format.hpp:215-274.  Bit-exact with
+ * the reference layout.  Host CSR -> host METCF on all host threads; device
+ * CSR -> device METCF built by CUDA kernels on `stream`. */
+int accspmm_metcf_from_csr(const accspmm_csr_t* csr, accspmm_metcf_t* metcf,
+                           void* stream);
+
+/* AdpBME<T>::CSR2AdpBME(csr, t_load, t_comp, t_write, target_num),
+ * include/format.hpp:340-429, computed from an existing METCF (the per-tile
+ * arrays are identical; the reference recomputes them).  Host or device, by
+ * metcf->space.  The reference's driver uses (3, 1, 2, 16),
+ * src/mma_tf32.cu:222. */
+int accspmm_adpbme_from_metcf(const accspmm_metcf_t* metcf, uint32_t t_load,
+                              uint32_t t_comp, uint32_t t_write,
+                              uint32_t target_num, accspmm_adpbme_t* adp,
+                              void* stream);
+
+/* balanceStrategy, include/utils.hpp:75-85: *adaptive = 1 when the window
+ * imbalance degree exceeds IMBALANCE_THRESHOLD (8).  Host or device. */
+int accspmm_balance_strategy(const accspmm_metcf_t* metcf, int* adaptive,
+                             void* stream);
+
+/* Number of C rows the adaptive path writes: max(8 G, rowIndices.back() + 8),
+ * src/mma_tf32.cu:112. */
+int accspmm_adaptive_c_rows(const accspmm_adpbme_t* adp, uint32_t* c_rows,
+                            void* stream);
+
+/* Copies between host and device (the H2D/D2H of src/mma_tf32.cu:53-68,
+ * :139-156).  The destination is library-owned.  A copy from or to host
+ * memory has completed when the call returns. */
+int accspmm_metcf_copy(const accspmm_metcf_t* src, int32_t dst_space,
+                       accspmm_metcf_t* dst, void* stream);
+int accspmm_csr_copy(const accspmm_csr_t* src, int32_t dst_space,
+                     accspmm_csr_t* dst, void* stream);
+int accspmm_coo_copy(const accspmm_coo_t* src, int32_t dst_space,
+                     accspmm_coo_t* dst, void* stream);
+int accspmm_adpbme_copy(const accspmm_adpbme_t* src, int32_t dst_space,
+                        accspmm_adpbme_t* dst, void* stream);
+
+void accspmm_coo_destroy(accspmm_coo_t* coo);
+void accspmm_csr_destroy(accspmm_csr_t* csr);
+void accspmm_metcf_destroy(accspmm_metcf_t* metcf);
+void accspmm_adpbme_destroy(accspmm_adpbme_t* adp);
+
+/* ---- SpMM ---------------------------------------------------------------- */
+/* TF32Compute::compute, include/tf32_comp.hpp:52-80 (kernels
+ * tf32_mma_kernel / tf32_mma_g512_kernel, include/mma_tf32.cuh:13-550), one
+ * launch, no timing loop.  C = decode(METCF) * B over all 8W rows; C is
+ * fully written (rows of empty windows become 0).  Device METCF, B, C. */
+int accspmm_spmm_tf32(const accspmm_metcf_t* metcf, const float* B, float* C,
+                      uint32_t K, int32_t precision, void* stream);
+
+/* TF32Compute::adpBalanceCompute, include/tf32_comp.hpp:82-113 (kernels
+ * tf32_mma_balance_kernel / _g128_kernel, include/mma_tf32.cuh:552-1042),
+ * one launch.  Load balance follows the AdpBME tile order; partial row
+ * windows are summed in a fixed order (no float atomics), so the result is
+ * deterministic.  C has c_rows rows (accspmm_adaptive_c_rows) and is
+ * overwritten, where the reference accumulated into a pre-zeroed C.  Needs
+ * 4 (rows/8 + 2) bytes of device scratch, allocated stream-ordered. */
+int accspmm_spmm_adaptive(const accspmm_adpbme_t* adp, const float* B,
+                          float* C, uint32_t c_rows, uint32_t K,
+                          int32_t precision, void* stream);
+
+/* The timing loop of TF32Compute::executeKernel, include/tf32_comp.hpp:33-46:
+ * `warmup` untimed launches, then `exe` launches between two CUDA events on
+ * `stream`; *avg_ms = elapsed / exe.  `adp` may be NULL (plain path). */
+int accspmm_time_spmm(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp,
+                      const float* B, float* C, uint32_t c_rows, uint32_t K,
+                      int32_t precision, int32_t warmup, int32_t exe,
+                      float* avg_ms, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ACCSPMM_H */

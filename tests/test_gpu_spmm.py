@@ -1,0 +1,264 @@
+"""GPU parity: device builders bit-exact with the reference layout, SpMM within
+the stated tolerances of the oracle, all through the C ABI."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from accspmm_gb300 import api, capi, synth
+from oracle import oracle
+from tests.helpers import (GOLD, TOL_3XTF32_VS_F64, TOL_TF32_VS_EMU, TOL_TF32_VS_F64, empty_dev,
+                           gold, max_row_rel, rel_fro, torch_dev)
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+OK_CASES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLD, "*.npz"))
+                  if int(np.load(p)["status"][0]) == 0)
+
+
+def csr_of_gold(g):
+    return dict(rows=int(g["dims"][0]), cols=int(g["dims"][1]), nnz=int(g["dims"][2]),
+                row_ptr=g["csr_row_ptr"], col_idx=g["csr_col_idx"], data=g["csr_data"])
+
+
+def device_metcf(csr):
+    d = api.DeviceCSR.upload(csr)
+    m = api.DeviceMETCF.from_csr(d)
+    torch.cuda.synchronize()
+    return m
+
+
+@pytest.mark.parametrize("name", OK_CASES)
+def test_device_builders_match_reference(name):
+    g = gold(name)
+    m = device_metcf(csr_of_gold(g))
+    h = m.to_numpy()
+    for k, gk in [("rwo", "m_rwo"), ("tc_offset", "m_tc_offset"), ("bits", "m_bits"),
+                  ("a2b", "m_a2b"), ("data", "m_data")]:
+        np.testing.assert_array_equal(h[k], g[gk], err_msg=k)
+    assert m.balance_strategy() == int(g["balance"][0])
+    if "a_group_offset" in g:
+        a = m.adpbme().to_numpy()
+        for k, gk in [("group_offset", "a_group_offset"), ("tc_offset", "a_tc_offset"),
+                      ("row_indices", "a_row_indices"), ("bits", "a_bits"), ("a2b", "a_a2b"),
+                      ("data", "a_data")]:
+            np.testing.assert_array_equal(a[k], g[gk], err_msg=k)
+        b = m.adpbme(2, 3, 5, 4).to_numpy()
+        np.testing.assert_array_equal(b["group_offset"], g["b_group_offset"])
+
+
+def test_device_csr_from_coo_matches_host():
+    g = gold("ragged_unsorted")
+    rows, cols = int(g["dims"][0]), int(g["dims"][1])
+    import ctypes as C
+    coo = api.coo_struct(rows, cols, g["coo_row"], g["coo_col"], g["coo_data"])
+    dcoo = capi.COO()
+    capi.call("accspmm_coo_copy", C.byref(coo.struct), capi.DEVICE, C.byref(dcoo), None)
+    dcsr = capi.CSR()
+    capi.call("accspmm_csr_from_coo", C.byref(dcoo), C.byref(dcsr), None)
+    hcsr = capi.CSR()
+    capi.call("accspmm_csr_copy", C.byref(dcsr), capi.HOST, C.byref(hcsr), None)
+    got = api.csr_to_numpy(hcsr)
+    np.testing.assert_array_equal(got["row_ptr"], g["csr_row_ptr"])
+    np.testing.assert_array_equal(got["col_idx"], g["csr_col_idx"])
+    np.testing.assert_array_equal(got["data"], g["csr_data"])
+    lib = capi.load()
+    for s, f in ((dcoo, lib.accspmm_coo_destroy), (dcsr, lib.accspmm_csr_destroy),
+                 (hcsr, lib.accspmm_csr_destroy)):
+        f(C.byref(s))
+
+
+@pytest.mark.parametrize("seed", [0, 3])
+def test_device_metcf_config1_and_unsorted(seed):
+    r, c, v = synth.powerlaw_symmetric(n=16384, seed=seed)
+    r, c, v = synth.expand_symmetric(r, c, v)
+    csr = api.csr_from_coo(16384, 16384, r, c, v)
+    o = oracle.metcf(16384, csr["row_ptr"], csr["col_idx"], csr["data"])
+    h = device_metcf(csr).to_numpy()
+    for k in ("rwo", "tc_offset", "bits", "a2b", "data"):
+        np.testing.assert_array_equal(h[k], o[k], err_msg=k)
+    # unsorted rows with duplicates
+    rng = np.random.default_rng(seed)
+    rows, cols, nnz = 2000, 3000, 40000
+    rr = np.sort(rng.integers(0, rows, nnz)).astype(np.uint32)
+    cc = rng.integers(0, cols, nnz).astype(np.uint32)
+    vv = rng.random(nnz, dtype=np.float32)
+    csr = api.csr_from_coo(rows, cols, rr, cc, vv)
+    o = oracle.metcf(rows, csr["row_ptr"], csr["col_idx"], csr["data"])
+    h = device_metcf(csr).to_numpy()
+    for k in ("rwo", "tc_offset", "bits", "a2b", "data"):
+        np.testing.assert_array_equal(h[k], o[k], err_msg=k)
+
+
+def spmm_plain(m, B, K, prec=capi.PREC_TF32):
+    dB = torch_dev(B)
+    dC = empty_dev(m.c_rows, K)
+    m.spmm(dB, dC, K, prec)
+    torch.cuda.synchronize()
+    return dC.cpu().numpy()[:m.c_rows]
+
+
+@pytest.mark.parametrize("name", OK_CASES)
+@pytest.mark.parametrize("K", [4, 32, 36, 64, 128, 200, 256, 516])
+def test_spmm_tf32_matches_oracle(name, K):
+    g = gold(name)
+    csr = csr_of_gold(g)
+    m = device_metcf(csr)
+    h = m.to_numpy()
+    B = np.random.default_rng(K).uniform(-1, 1, (csr["cols"], K)).astype(np.float32)
+    got = spmm_plain(m, B, K)
+    c64 = oracle.spmm_metcf_f64(h, csr["cols"], B)
+    emu = oracle.spmm_metcf_tf32(h, csr["cols"], B)
+    assert got.shape == c64.shape
+    assert np.isfinite(got).all()
+    assert rel_fro(got, emu) < TOL_TF32_VS_EMU
+    assert rel_fro(got, c64) < TOL_TF32_VS_F64
+    # rows past the last matrix row (window padding) are written as zeros
+    assert not got[csr["rows"]:].any()
+
+
+@pytest.mark.parametrize("K", [32, 64, 128, 256])
+def test_spmm_3xtf32_matches_fp64(K):
+    g = gold("plsym1000")
+    csr = csr_of_gold(g)
+    m = device_metcf(csr)
+    h = m.to_numpy()
+    B = synth.dense_scaled_normal(csr["cols"], K, seed=K)
+    got = spmm_plain(m, B, K, capi.PREC_3XTF32)
+    c64 = oracle.spmm_metcf_f64(h, csr["cols"], B)
+    assert rel_fro(got, c64) < TOL_3XTF32_VS_F64
+    assert max_row_rel(got, c64) < 1e-5
+    tf = spmm_plain(m, B, K, capi.PREC_TF32)
+    assert rel_fro(tf, c64) > 10 * rel_fro(got, c64)
+
+
+def test_spmm_config1_against_csr_fp64():
+    r, c, v = synth.powerlaw_symmetric(n=16384, seed=0)
+    r, c, v = synth.expand_symmetric(r, c, v)
+    csr = api.csr_from_coo(16384, 16384, r, c, v)
+    m = device_metcf(csr)
+    B = synth.dense_uniform(16384, 128, seed=0)
+    got = spmm_plain(m, B, 128)
+    ref = oracle.spmm_csr_f64(csr["row_ptr"], csr["col_idx"], csr["data"], B)
+    assert rel_fro(got[:16384], ref) < TOL_TF32_VS_F64
+    got3 = spmm_plain(m, B, 128, capi.PREC_3XTF32)
+    assert rel_fro(got3[:16384], ref) < TOL_3XTF32_VS_F64
+
+
+@pytest.mark.parametrize("name", ["longwin", "plsym1000", "rand203", "ragged_unsorted"])
+@pytest.mark.parametrize("prec", [capi.PREC_TF32, capi.PREC_3XTF32])
+def test_adaptive_equals_plain(name, prec):
+    """The adaptive entry point gives bit-identical rows to the plain one and
+    zeros in the extra rows of its larger C."""
+    g = gold(name)
+    csr = csr_of_gold(g)
+    m = device_metcf(csr)
+    a = m.adpbme()
+    c_rows = a.c_rows()
+    ah = a.to_numpy()
+    assert c_rows == max(8 * (len(ah["group_offset"]) - 1), int(ah["row_indices"][-1]) + 8)
+    K = 64
+    B = np.random.default_rng(1).uniform(-1, 1, (csr["cols"], K)).astype(np.float32)
+    dB = torch_dev(B)
+    dC = empty_dev(c_rows, K)
+    a.spmm(dB, dC, c_rows, K, prec)
+    torch.cuda.synchronize()
+    ad = dC.cpu().numpy()[:c_rows]
+    pl = spmm_plain(m, B, K, prec)
+    n = min(c_rows, pl.shape[0])
+    np.testing.assert_array_equal(ad[:n], pl[:n])
+    assert not ad[n:].any()
+
+
+def test_spmm_deterministic():
+    g = gold("longwin")
+    csr = csr_of_gold(g)
+    m = device_metcf(csr)
+    B = np.random.default_rng(2).uniform(-1, 1, (csr["cols"], 128)).astype(np.float32)
+    a = spmm_plain(m, B, 128)
+    b = spmm_plain(m, B, 128)
+    np.testing.assert_array_equal(a, b)
+
+
+def test_spmm_empty_matrix_writes_zeros():
+    csr = dict(rows=20, cols=20, nnz=0, row_ptr=np.zeros(21, np.uint32),
+               col_idx=np.zeros(0, np.uint32), data=np.zeros(0, np.float32))
+    m = device_metcf(csr)
+    assert m.struct.num_tiles == 0
+    got = spmm_plain(m, np.ones((20, 32), np.float32), 32)
+    assert got.shape == (24, 32) and not got.any()
+
+
+def test_spmm_rejects_bad_arguments():
+    g = gold("kat10")
+    m = device_metcf(csr_of_gold(g))
+    dB = torch_dev(np.ones((10, 32), np.float32))
+    dC = empty_dev(16, 32)
+    with pytest.raises(capi.AccSpmmError) as e:
+        m.spmm(dB, dC, 30)
+    assert e.value.status == capi.ERROR_INVALID_VALUE
+    with pytest.raises(capi.AccSpmmError):
+        m.spmm(dB.data_ptr() + 4, dC, 32)
+    with pytest.raises(capi.AccSpmmError):
+        m.spmm(dB, dC, 32, precision=7)
+
+
+def test_row_identical_b_regime():
+    """With every B row equal to v, C = rowsum(A) v^T: the only regime in which
+    the reference kernels' output is trustworthy."""
+    g = gold("plsym1000")
+    csr = csr_of_gold(g)
+    m = device_metcf(csr)
+    v = np.random.default_rng(3).uniform(-1, 1, 64).astype(np.float32)
+    B = np.tile(v, (csr["cols"], 1))
+    got = spmm_plain(m, B, 64)
+    rs = np.add.reduceat(csr["data"].astype(np.float64),
+                         csr["row_ptr"][:-1].astype(np.int64)) if csr["nnz"] else None
+    counts = np.diff(csr["row_ptr"].astype(np.int64))
+    rs = np.where(counts > 0, rs, 0.0)
+    ref = np.outer(rs, v.astype(np.float64))
+    assert rel_fro(got[:csr["rows"]], ref) < TOL_TF32_VS_F64
+
+
+@pytest.mark.slow
+def test_scale_workload_properties():
+    """The 1M-row workload at K=128: size-independent checks against an FP64
+    CSR evaluation of row sums (C 1 = A (B 1)), linearity in B, determinism,
+    and exact agreement of the adaptive and plain entry points."""
+    rp, ci, vals = synth.powerlaw_local(n=1 << 20, seed=0)
+    n = 1 << 20
+    csr = dict(rows=n, cols=n, nnz=len(ci), row_ptr=rp, col_idx=ci, data=vals)
+    m = device_metcf(csr)
+    K = 128
+    B1 = torch.rand((n, K), device="cuda") * 2 - 1
+    B2 = torch.rand((n, K), device="cuda") * 2 - 1
+    C1 = empty_dev(m.c_rows, K)
+    C2 = empty_dev(m.c_rows, K)
+    C12 = empty_dev(m.c_rows, K)
+    m.spmm(B1, C1, K)
+    m.spmm(B2, C2, K)
+    B12 = (B1 + B2).contiguous()
+    m.spmm(B12, C12, K)
+    torch.cuda.synchronize()
+    lin = (C12 - C1 - C2).norm() / C12.norm()
+    assert lin.item() < 2e-3
+    # row sums through an FP64 CSR SpMV
+    bsum = B1.double().sum(1).cpu().numpy()
+    row_of = np.repeat(np.arange(n), np.diff(rp.astype(np.int64)))
+    ref = np.bincount(row_of, weights=vals.astype(np.float64) * bsum[ci], minlength=n)
+    got = C1.double().sum(1).cpu().numpy()[:n]
+    assert rel_fro(got, ref) < TOL_TF32_VS_F64
+    C1b = empty_dev(m.c_rows, K)
+    m.spmm(B1, C1b, K)
+    torch.cuda.synchronize()
+    assert torch.equal(C1, C1b)
+    a = m.adpbme()
+    cr = a.c_rows()
+    Ca = empty_dev(cr, K)
+    a.spmm(B1, Ca, cr, K)
+    torch.cuda.synchronize()
+    k = min(cr, m.c_rows)
+    assert torch.equal(Ca[:k], C1[:k])
