@@ -11,7 +11,8 @@ import re
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
-LIB_PATH = os.path.join(PKG, "libaccspmm.so")
+# ACCSPMM_LIB selects another build of the library (same ABI)
+LIB_PATH = os.environ.get("ACCSPMM_LIB") or os.path.join(PKG, "libaccspmm.so")
 HEADER = os.path.join(ROOT, "include", "accspmm.h")
 
 u32 = C.c_uint32

@@ -23,54 +23,18 @@
 // 71-79).  Tile metadata is fetched a batch ahead with one coalesced load.
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 
 #include "common.hpp"
 #include "device_util.cuh"
+#include "spmm_common.cuh"
 #include "spmm_internal.hpp"
 
 namespace accspmm {
 
 namespace {
 
-constexpr int kNW = 8;  // warps per CTA
-
-struct SpmmArgs {
-    const uint32_t* rwo;
-    const uint32_t* tc_offset;
-    const uint64_t* bits;
-    const uint32_t* a2b;
-    const float* vals;
-    const float* B;
-    float* C;
-    uint32_t W;         // windows covered (C has 8W rows)
-    uint32_t cols;      // rows of B
-    uint32_t K;         // columns of B and C
-    uint32_t wb;        // windows per CTA
-    uint32_t n_slices;  // feature slices
-};
-
-__device__ __forceinline__ uint32_t f2tf32(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return r;
-}
-
-__device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2,
-                                         uint32_t a3, uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 "
-        "{%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-__device__ __forceinline__ float4 ldg_f4(const float* p) {
-    return __ldg(reinterpret_cast<const float4*>(p));
-}
-
-__device__ __forceinline__ float comp(const float4& v, int j) {
-    return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w;
-}
+constexpr int kNW = 8;  // warps per CTA of the register-direct kernel
 
 __device__ __forceinline__ uint64_t shfl_u64(uint64_t v, int src) {
     uint32_t lo = __shfl_sync(0xffffffffu, uint32_t(v), src);
@@ -78,52 +42,8 @@ __device__ __forceinline__ uint64_t shfl_u64(uint64_t v, int src) {
     return (uint64_t(hi) << 32) | lo;
 }
 
-// Sparse value of tile element `bit` (row-major 8x8), 0 if absent.
-__device__ __forceinline__ float tile_value(uint64_t bm, uint32_t off, const float* __restrict__ vals,
-                                            uint32_t bit) {
-    if (!((bm >> bit) & 1ull)) return 0.0f;
-    uint64_t below = bm & ((2ull << bit) - 1ull);  // 2 << 63 wraps to 0: all bits
-    return __ldg(vals + off + __popcll(below) - 1);
-}
-
-// Accumulator layout helpers.  H = FS / 32 float4 per B row per lane;
-// NM = MMAs per tile.  acc[m][0..3] follow the m16n8 D fragment: [0] (g, 2tq),
-// [1] (g, 2tq+1), [2] (g+8, 2tq), [3] (g+8, 2tq+1); m-row -> feature below.
-template <int H>
-struct Layout {
-    static constexpr int NM = H >= 2 ? 2 * H : 2;
-    // float4 of output row n = 2tq + p, feature group h (features 32h + 4g + 0..3)
-    __device__ static __forceinline__ float4 get(const float (&acc)[NM][4], int p, int h) {
-        if constexpr (H >= 2) {
-            const int hp = h >> 1, q = h & 1;
-            return make_float4(acc[hp * 4 + 0][p + 2 * q], acc[hp * 4 + 1][p + 2 * q],
-                               acc[hp * 4 + 2][p + 2 * q], acc[hp * 4 + 3][p + 2 * q]);
-        } else {
-            return make_float4(acc[0][p], acc[1][p], acc[0][p + 2], acc[1][p + 2]);
-        }
-    }
-};
-
-template <int FS>
-__device__ __forceinline__ void store_rows(float* __restrict__ C, uint32_t K, uint32_t row0,
-                                           uint32_t f0, int g, int tq, const float4 (&out)[2][FS / 32]) {
-#pragma unroll
-    for (int p = 0; p < 2; ++p) {
-        float* rowp = C + size_t(row0 + 2 * tq + p) * K;
-#pragma unroll
-        for (int h = 0; h < FS / 32; ++h) {
-            uint32_t f = f0 + 32 * h + 4 * g;
-            if (f < K) __stcs(reinterpret_cast<float4*>(rowp + f), out[p][h]);
-        }
-    }
-}
-
-// Shared-memory partial slot: [8 rows][FS] floats.
-template <int FS>
-__device__ __forceinline__ float* slot_ptr(float* part, int slot) {
-    return part + size_t(slot) * 8 * FS;
-}
-
+// Register-direct kernel: each lane loads its B fragments straight from
+// global memory, a batch of U tiles at a time.
 template <int FS, int PREC>
 __global__ void __launch_bounds__(kNW * 32, 2) spmm_window_kernel(const SpmmArgs a) {
     constexpr int H = FS / 32;
@@ -132,75 +52,33 @@ __global__ void __launch_bounds__(kNW * 32, 2) spmm_window_kernel(const SpmmArgs
     constexpr int U = H >= 4 ? 2 : (H == 2 ? 4 : 8);  // tiles per batch
     constexpr int MA = (8 * U + 31) / 32;             // a2b registers per lane
 
-    extern __shared__ float smem[];
+    extern __shared__ __align__(16) float smem[];
     float* part = smem;  // [2 * kNW] slots
     uint32_t* s_rwo = reinterpret_cast<uint32_t*>(smem + 2 * kNW * 8 * FS);
+    Block<FS, kNW> blk;
+    blk.init(a, s_rwo, part);
+    const int lane = blk.lane, g = blk.g, tq = blk.tq;
+    const uint32_t tb = blk.bound(blk.warp), te = blk.bound(blk.warp + 1);
 
-    const uint32_t wbk = blockIdx.x / a.n_slices;
-    const uint32_t slice = blockIdx.x - wbk * a.n_slices;
-    const uint32_t w0 = wbk * a.wb;
-    const uint32_t w1 = min(w0 + a.wb, a.W);
-    const uint32_t nwin = w1 - w0;
-    const uint32_t f0 = slice * FS;
-    for (uint32_t i = threadIdx.x; i <= nwin; i += blockDim.x) s_rwo[i] = a.rwo[w0 + i];
-    __syncthreads();
-
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int g = lane >> 2, tq = lane & 3;
-    const uint32_t t_begin = s_rwo[0];
-    const uint32_t t_total = s_rwo[nwin] - t_begin;
-    auto bound = [&](int i) -> uint32_t {
-        return t_begin + uint32_t((uint64_t(t_total) * uint32_t(i)) / kNW);
-    };
-    const uint32_t tb = bound(warp), te = bound(warp + 1);
-
-    // feature offsets of this lane's float4s and whether they are inside K
     bool fok[H];
 #pragma unroll
-    for (int h = 0; h < H; ++h) fok[h] = f0 + 32 * h + 4 * g < a.K;
+    for (int h = 0; h < H; ++h) fok[h] = blk.f0 + 32 * h + 4 * g < a.K;
 
     if (tb < te) {
-        // window (local index) containing tb
-        uint32_t wl = 0;
-        for (uint32_t jb = 0; jb < nwin; jb += 32) {
-            const uint32_t j = jb + uint32_t(lane);
-            const bool in = j < nwin && s_rwo[j] <= tb && tb < s_rwo[j + 1];
-            const unsigned bal = __ballot_sync(0xffffffffu, in);
-            if (bal) wl = jb + uint32_t(__ffs(bal) - 1);
-        }
-        uint32_t next_bound = s_rwo[wl + 1];
+        uint32_t wl = blk.window_of(tb);
+        uint32_t next_bound = blk.s_rwo[wl + 1];
         bool first_win = true;
         float acc[NM][4];
 #pragma unroll
         for (int m = 0; m < NM; ++m) acc[m][0] = acc[m][1] = acc[m][2] = acc[m][3] = 0.f;
 
-        auto flush = [&](uint32_t wloc) {
-            const uint32_t rb = s_rwo[wloc], re = s_rwo[wloc + 1];
-            float4 out[2][H];
-#pragma unroll
-            for (int p = 0; p < 2; ++p)
-#pragma unroll
-                for (int h = 0; h < H; ++h) out[p][h] = L::get(acc, p, h);
-            if (rb >= tb && re <= te) {
-                store_rows<FS>(a.C, a.K, (w0 + wloc) * kWin, f0, g, tq, out);
-            } else {
-                float* sp = slot_ptr<FS>(part, 2 * warp + (first_win ? 0 : 1));
-#pragma unroll
-                for (int p = 0; p < 2; ++p)
-#pragma unroll
-                    for (int h = 0; h < H; ++h)
-                        *reinterpret_cast<float4*>(sp + (2 * tq + p) * FS + 32 * h + 4 * g) = out[p][h];
-            }
-        };
-
-        // metadata of a batch of U tiles starting at t
         uint32_t ma[MA];
         uint64_t mb;
         uint32_t mo;
         auto load_meta = [&](uint32_t t) {
 #pragma unroll
             for (int j = 0; j < MA; ++j) {
-                uint32_t e = 32 * j + lane;            // entry within the batch
+                uint32_t e = 32 * j + lane;
                 uint32_t tile = t + e / 8;
                 ma[j] = (e < 8 * U && tile < te) ? __ldg(a.a2b + size_t(t) * 8 + e) : kPad;
             }
@@ -211,9 +89,10 @@ __global__ void __launch_bounds__(kNW * 32, 2) spmm_window_kernel(const SpmmArgs
         };
         load_meta(tb);
 
-        const uint32_t bit0 = uint32_t(g) * 8 + uint32_t(tq), bit1 = bit0 + 4;
+        BitDecode dec;
+        dec.init(g, tq);
+        const float* Bl = a.B + blk.f0 + 4 * g;
         for (uint32_t t = tb; t < te; t += U) {
-            // gather: A values and B rows of the whole batch
             float av0[U], av1[U];
             float4 r0[U][H], r1[U][H];
 #pragma unroll
@@ -222,15 +101,18 @@ __global__ void __launch_bounds__(kNW * 32, 2) spmm_window_kernel(const SpmmArgs
                 const uint32_t i1 = __shfl_sync(0xffffffffu, ma[(8 * u) / 32], (8 * u + tq + 4) & 31);
                 const uint64_t bm = shfl_u64(mb, u);
                 const uint32_t to = __shfl_sync(0xffffffffu, mo, u);
-                av0[u] = tile_value(bm, to, a.vals, bit0);
-                av1[u] = tile_value(bm, to, a.vals, bit1);
+                uint32_t x0, x1;
+                bool q0, q1;
+                dec.decode(bm, x0, x1, q0, q1);
+                av0[u] = q0 ? ldg_f32_ordered(a.vals + to + x0) : 0.f;
+                av1[u] = q1 ? ldg_f32_ordered(a.vals + to + x1) : 0.f;
                 const bool v0 = i0 < a.cols, v1 = i1 < a.cols;
-                const float* p0 = a.B + size_t(v0 ? i0 : 0) * a.K + f0 + 4 * g;
-                const float* p1 = a.B + size_t(v1 ? i1 : 0) * a.K + f0 + 4 * g;
+                const float* p0 = Bl + size_t(v0 ? i0 : 0) * a.K;
+                const float* p1 = Bl + size_t(v1 ? i1 : 0) * a.K;
 #pragma unroll
                 for (int h = 0; h < H; ++h) {
-                    r0[u][h] = (v0 && fok[h]) ? ldg_f4(p0 + 32 * h) : make_float4(0.f, 0.f, 0.f, 0.f);
-                    r1[u][h] = (v1 && fok[h]) ? ldg_f4(p1 + 32 * h) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    r0[u][h] = (v0 && fok[h]) ? ldg_f4_ordered(p0 + 32 * h) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    r1[u][h] = (v1 && fok[h]) ? ldg_f4_ordered(p1 + 32 * h) : make_float4(0.f, 0.f, 0.f, 0.f);
                 }
             }
             if (t + U < te) load_meta(t + U);
@@ -239,104 +121,20 @@ __global__ void __launch_bounds__(kNW * 32, 2) spmm_window_kernel(const SpmmArgs
                 const uint32_t tt = t + u;
                 if (tt >= te) break;
                 if (tt >= next_bound) {
-                    flush(wl);
+                    blk.flush(a, acc, wl, tb, te, first_win);
                     first_win = false;
 #pragma unroll
                     for (int m = 0; m < NM; ++m) acc[m][0] = acc[m][1] = acc[m][2] = acc[m][3] = 0.f;
-                    while (s_rwo[wl + 1] <= tt) ++wl;
-                    next_bound = s_rwo[wl + 1];
+                    while (blk.s_rwo[wl + 1] <= tt) ++wl;
+                    next_bound = blk.s_rwo[wl + 1];
                 }
-                if constexpr (PREC == ACCSPMM_PREC_TF32) {
-                    const uint32_t b0 = f2tf32(av0[u]), b1 = f2tf32(av1[u]);
-#pragma unroll
-                    for (int m = 0; m < NM; ++m) {
-                        const int j = m & 3;
-                        float x0, x1, x2, x3;
-                        if constexpr (H >= 2) {
-                            const int hp = m >> 2;
-                            x0 = comp(r0[u][2 * hp], j); x1 = comp(r0[u][2 * hp + 1], j);
-                            x2 = comp(r1[u][2 * hp], j); x3 = comp(r1[u][2 * hp + 1], j);
-                        } else {
-                            x0 = comp(r0[u][0], m); x1 = comp(r0[u][0], m + 2);
-                            x2 = comp(r1[u][0], m); x3 = comp(r1[u][0], m + 2);
-                        }
-                        mma_tf32(acc[m], f2tf32(x0), f2tf32(x1), f2tf32(x2), f2tf32(x3), b0, b1);
-                    }
-                } else {
-                    // 3xTF32 (Ootomo & Yokota 2022): x = hi + lo with hi, lo TF32;
-                    // d = B_lo*A_hi + B_hi*A_lo + B_hi*A_hi per tile, then added to
-                    // the FP32 accumulators outside the tensor core.
-                    const uint32_t bh0 = f2tf32(av0[u]), bh1 = f2tf32(av1[u]);
-                    const uint32_t bl0 = f2tf32(av0[u] - __uint_as_float(bh0));
-                    const uint32_t bl1 = f2tf32(av1[u] - __uint_as_float(bh1));
-#pragma unroll
-                    for (int m = 0; m < NM; ++m) {
-                        const int j = m & 3;
-                        float x[4];
-                        if constexpr (H >= 2) {
-                            const int hp = m >> 2;
-                            x[0] = comp(r0[u][2 * hp], j); x[1] = comp(r0[u][2 * hp + 1], j);
-                            x[2] = comp(r1[u][2 * hp], j); x[3] = comp(r1[u][2 * hp + 1], j);
-                        } else {
-                            x[0] = comp(r0[u][0], m); x[1] = comp(r0[u][0], m + 2);
-                            x[2] = comp(r1[u][0], m); x[3] = comp(r1[u][0], m + 2);
-                        }
-                        uint32_t hi[4], lo[4];
-#pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            hi[q] = f2tf32(x[q]);
-                            lo[q] = f2tf32(x[q] - __uint_as_float(hi[q]));
-                        }
-                        float d[4] = {0.f, 0.f, 0.f, 0.f};
-                        mma_tf32(d, lo[0], lo[1], lo[2], lo[3], bh0, bh1);
-                        mma_tf32(d, hi[0], hi[1], hi[2], hi[3], bl0, bl1);
-                        mma_tf32(d, hi[0], hi[1], hi[2], hi[3], bh0, bh1);
-                        acc[m][0] += d[0]; acc[m][1] += d[1]; acc[m][2] += d[2]; acc[m][3] += d[3];
-                    }
-                }
+                tile_mma<H, PREC>(acc, r0[u], r1[u], av0[u], av1[u]);
             }
         }
-        flush(wl);
+        blk.flush(a, acc, wl, tb, te, first_win);
     }
     __syncthreads();
-
-    // windows cut by piece boundaries: sum the slots in warp order; empty
-    // windows: zeros
-    auto warp_of = [&](uint32_t t) -> int {
-        int i = kNW - 1;
-        while (i > 0 && bound(i) > t) --i;
-        return i;
-    };
-    for (uint32_t wloc = warp; wloc < nwin; wloc += kNW) {
-        const uint32_t rb = s_rwo[wloc], re = s_rwo[wloc + 1];
-        float4 out[2][H];
-        if (rb == re) {
-#pragma unroll
-            for (int p = 0; p < 2; ++p)
-#pragma unroll
-                for (int h = 0; h < H; ++h) out[p][h] = make_float4(0.f, 0.f, 0.f, 0.f);
-        } else {
-            const int ia = warp_of(rb), ib = warp_of(re - 1);
-            if (ia == ib) continue;  // stored by its warp
-#pragma unroll
-            for (int p = 0; p < 2; ++p)
-#pragma unroll
-                for (int h = 0; h < H; ++h) out[p][h] = make_float4(0.f, 0.f, 0.f, 0.f);
-            for (int i = ia; i <= ib; ++i) {
-                const uint32_t bi = bound(i);
-                if (bi == bound(i + 1)) continue;  // empty piece
-                const float* sp = slot_ptr<FS>(part, 2 * i + (rb <= bi ? 0 : 1));
-#pragma unroll
-                for (int p = 0; p < 2; ++p)
-#pragma unroll
-                    for (int h = 0; h < H; ++h) {
-                        float4 v = *reinterpret_cast<const float4*>(sp + (2 * tq + p) * FS + 32 * h + 4 * g);
-                        out[p][h].x += v.x; out[p][h].y += v.y; out[p][h].z += v.z; out[p][h].w += v.w;
-                    }
-            }
-        }
-        store_rows<FS>(a.C, a.K, (w0 + wloc) * kWin, f0, g, tq, out);
-    }
+    blk.finish(a);
 }
 
 // rwo[w] = first tile whose window (row_indices / 8) is >= w, for w in
@@ -356,32 +154,46 @@ __global__ void rwo_from_row_indices_kernel(const uint32_t* __restrict__ ri, uin
     for (uint32_t w = lo; w <= hi && w <= Weff; ++w) rwo[w] = t;
 }
 
+enum KernelKind { kDirect = 0, kPipe = 1 };
+
 struct Config {
+    int kernel;
     int fs;
+    int nw;
+    int hints;
     uint32_t wb;
+    uint32_t slice_major;
 };
+
+int env_int(const char* name, int dflt) {
+    const char* e = std::getenv(name);
+    return e && *e ? std::atoi(e) : dflt;
+}
 
 Config choose_config(uint32_t W, uint32_t K) {
     Config c;
+    c.kernel = kDirect;
+    if (const char* e = std::getenv("ACCSPMM_KERNEL")) c.kernel = std::strcmp(e, "pipe") == 0 ? kPipe : kDirect;
     c.fs = K <= 32 ? 32 : 64;
-    if (const char* e = std::getenv("ACCSPMM_FS")) {
-        int v = std::atoi(e);
-        if (v == 32 || v == 64 || v == 128) c.fs = v;
-    }
+    int fs = env_int("ACCSPMM_FS", 0);
+    if (fs == 32 || fs == 64 || fs == 128) c.fs = fs;
+    c.nw = env_int("ACCSPMM_NW", c.fs == 32 ? 8 : 4) == 4 ? 4 : 8;
+    if (c.kernel == kPipe && c.fs >= 64) c.nw = 4;  // stage ring must fit in shared memory
+    c.hints = env_int("ACCSPMM_HINTS", 1) ? 1 : 0;
     uint32_t slices = (K + c.fs - 1) / c.fs;
     // enough CTAs to fill every SM several times over, 4..32 windows each
     uint64_t want = uint64_t(sm_count()) * 16;
     uint64_t wb = (uint64_t(W) * slices + want - 1) / want;
     c.wb = uint32_t(std::min<uint64_t>(32, std::max<uint64_t>(4, wb)));
-    if (const char* e = std::getenv("ACCSPMM_WB")) {
-        int v = std::atoi(e);
-        if (v >= 1 && v <= 256) c.wb = uint32_t(v);
-    }
+    int wbe = env_int("ACCSPMM_WB", 0);
+    if (wbe >= 1 && wbe <= 1024) c.wb = uint32_t(wbe);
+    c.slice_major = 0;
+    if (const char* e = std::getenv("ACCSPMM_ORDER")) c.slice_major = std::strcmp(e, "slice") == 0;
     return c;
 }
 
 template <int FS, int PREC>
-int launch_fs(const SpmmArgs& a, cudaStream_t s) {
+int launch_direct(const SpmmArgs& a, cudaStream_t s) {
     const size_t smem = size_t(2 * kNW * 8 * FS) * 4 + size_t(a.wb + 1) * 4;
     static unsigned attr_set = 0;  // one bit per device
     int dev = 0;
@@ -391,7 +203,7 @@ int launch_fs(const SpmmArgs& a, cudaStream_t s) {
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
         attr_set |= 1u << dev;
     }
-    const uint64_t grid = uint64_t((a.W + a.wb - 1) / a.wb) * a.n_slices;
+    const uint64_t grid = uint64_t(a.n_wblocks) * a.n_slices;
     if (grid == 0) return ACCSPMM_SUCCESS;
     if (grid > 0x7FFFFFFFull) ACC_FAIL(ACCSPMM_ERROR_OVERFLOW, "grid too large");
     spmm_window_kernel<FS, PREC><<<unsigned(grid), kNW * 32, smem, s>>>(a);
@@ -423,12 +235,14 @@ int spmm_window_launch(const uint32_t* rwo, const uint32_t* tc_offset, const uin
     // matrix into the same pieces and sum partial windows in the same order
     Config cfg = choose_config(w_cfg, K);
     SpmmArgs a{rwo, tc_offset, bits, a2b, vals, B, C, W, cols, K, cfg.wb,
-               (K + uint32_t(cfg.fs) - 1) / uint32_t(cfg.fs)};
+               (K + uint32_t(cfg.fs) - 1) / uint32_t(cfg.fs), (W + cfg.wb - 1) / cfg.wb,
+               cfg.slice_major};
+    if (cfg.kernel == kPipe) return launch_pipe(a, cfg.fs, precision, cfg.nw, cfg.hints, s);
     const bool x3 = precision == ACCSPMM_PREC_3XTF32;
     switch (cfg.fs) {
-        case 32: return x3 ? launch_fs<32, ACCSPMM_PREC_3XTF32>(a, s) : launch_fs<32, ACCSPMM_PREC_TF32>(a, s);
-        case 64: return x3 ? launch_fs<64, ACCSPMM_PREC_3XTF32>(a, s) : launch_fs<64, ACCSPMM_PREC_TF32>(a, s);
-        default: return x3 ? launch_fs<128, ACCSPMM_PREC_3XTF32>(a, s) : launch_fs<128, ACCSPMM_PREC_TF32>(a, s);
+        case 32: return x3 ? launch_direct<32, ACCSPMM_PREC_3XTF32>(a, s) : launch_direct<32, ACCSPMM_PREC_TF32>(a, s);
+        case 64: return x3 ? launch_direct<64, ACCSPMM_PREC_3XTF32>(a, s) : launch_direct<64, ACCSPMM_PREC_TF32>(a, s);
+        default: return x3 ? launch_direct<128, ACCSPMM_PREC_3XTF32>(a, s) : launch_direct<128, ACCSPMM_PREC_TF32>(a, s);
     }
 }
 

@@ -40,8 +40,8 @@ UNIT = "GFLOP/s"
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
-    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--steps", type=int, default=300)
+    p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--k", type=int, default=128)
     p.add_argument("--n", type=int, default=1 << 20)
@@ -50,6 +50,9 @@ def parse():
     p.add_argument("--no-sweep", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-host-build", action="store_true")
+    p.add_argument("--profile", type=int, default=0, metavar="LAUNCHES",
+                   help="only build METCF on the GPU and run LAUNCHES plain SpMM launches "
+                        "(no timing): the command profiled by ncu")
     return p.parse_args()
 
 
@@ -88,7 +91,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -189,14 +192,30 @@ def run_reference(args):
     from oracle import oracle
     threads = oracle.omp_max_threads()
     C = np.zeros((args.n, args.k), np.float32)
-    for _ in range(max(args.warmup, 1)):
-        oracle.spmm_csr_f32_omp(rp, ci, v, B, C, threads=threads)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        oracle.spmm_csr_f32_omp(rp, ci, v, B, C, threads=threads)
+    oracle.spmm_csr_f32_omp(rp, ci, v, B, C, threads=threads)
+    t_full = time.perf_counter() - t0
+    # each step is a contiguous slice of rows, sized so that the whole run
+    # stays near a minute of CPU time
+    frac = min(1.0, 60.0 / (max(args.steps + args.warmup, 1) * max(t_full, 1e-6)))
+    rows_per_step = max(1024, int(args.n * frac))
+    starts = [(i * rows_per_step) % args.n for i in range(args.warmup + args.steps)]
+
+    def run(i):
+        r0 = starts[i]
+        r1 = min(args.n, r0 + rows_per_step)
+        oracle.spmm_csr_f32_omp(rp, ci, v, B, C, row_begin=r0, row_end=r1, threads=threads)
+        return int(rp[r1]) - int(rp[r0])
+
+    for i in range(args.warmup):
+        run(i)
+    work = 0
+    t0 = time.perf_counter()
+    for i in range(args.warmup, args.warmup + args.steps):
+        work += run(i)
     el = time.perf_counter() - t0
     ms = el / args.steps * 1e3
-    gf = 2.0 * len(ci) * args.k / (ms * 1e-3) / 1e9
+    gf = 2.0 * work * args.k / el / 1e9
     out = {
         "metric": METRIC, "value": round(gf, 2), "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
@@ -205,7 +224,8 @@ def run_reference(args):
         "config": {"workload": workload_name(args.n, args.k), "n_rows": args.n, "nnz": int(len(ci)),
                    "K": args.k, "path": "CPU CSR SpMM (oracle port; the reference has no CPU SpMM)"},
         "cpu_baseline": {"value": round(gf, 2), "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"full matrix per step, {args.steps} steps"},
+                         "sample": f"{rows_per_step} consecutive rows per step (of {args.n}), "
+                                   f"{args.steps} steps"},
         "e2e": {"value": round(gf, 2), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
@@ -246,6 +266,15 @@ def run_ours(args):
         api.metcf_from_csr(csr)
         host_build_ms = (time.perf_counter() - t0) * 1e3
     T, W = m.struct.num_tiles, m.struct.num_windows
+    if args.profile:
+        gen = torch.Generator(device=dev).manual_seed(args.seed)
+        B = torch.rand((n, K), device=dev, generator=gen) * 2 - 1
+        C = torch.empty((m.c_rows, K), device=dev)
+        for _ in range(args.profile):
+            m.spmm(B, C, K, prec, stream)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_launches": args.profile, "K": K, "tiles": int(T)}))
+        return
     adaptive = m.balance_strategy(stream)
     adp, G = None, None
     if adaptive:

@@ -262,3 +262,21 @@ def test_scale_workload_properties():
     torch.cuda.synchronize()
     k = min(cr, m.c_rows)
     assert torch.equal(Ca[:k], C1[:k])
+
+
+def test_tf32_rounding_is_rna_bit_exact():
+    """With A = I, C = rna_tf32(B) exactly (include/ptx_tf32.hpp:19-24 rounds
+    both operands with cvt.rna); B covers exact ties in both signs."""
+    n, K = 64, 32
+    csr = dict(rows=n, cols=n, nnz=n, row_ptr=np.arange(n + 1, dtype=np.uint32),
+               col_idx=np.arange(n, dtype=np.uint32), data=np.ones(n, np.float32))
+    m = device_metcf(csr)
+    rng = np.random.default_rng(9)
+    bits = rng.integers(0x30000000, 0x50000000, size=(n, K), dtype=np.uint32)
+    bits[:, :8] = (bits[:, :8] & 0xFFFFE000) | 0x1000          # ties
+    bits[:, 8:12] = (bits[:, 8:12] & 0xFFFFE000) | 0x0FFF      # just below
+    bits[::2] |= 0x80000000                                     # negatives
+    B = bits.view(np.float32)
+    got = spmm_plain(m, B, K)[:n]
+    want = np.vectorize(oracle.tf32_rna, otypes=[np.float32])(B)
+    np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
