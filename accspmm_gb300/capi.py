@@ -85,6 +85,7 @@ _SIGS = {
     "accspmm_adpbme_destroy": ([C.POINTER(ADPBME)], None),
     "accspmm_spmm_tf32": ([C.POINTER(METCF), vp, vp, u32, i32, vp], C.c_int),
     "accspmm_spmm_adaptive": ([C.POINTER(ADPBME), vp, vp, u32, u32, i32, vp], C.c_int),
+    "accspmm_device_status": ([vp], C.c_int),
     "accspmm_time_spmm": ([C.POINTER(METCF), C.POINTER(ADPBME), vp, vp, u32, u32, i32, i32, i32,
                            f32p, vp], C.c_int),
 }

@@ -316,6 +316,11 @@ int accspmm_spmm_adaptive(const accspmm_adpbme_t* adp, const float* B, float* C,
     return spmm_adaptive_impl(adp, B, C, c_rows, K, precision, stream);
 }
 
+int accspmm_device_status(void* stream) {
+    clear_error();
+    return device_status_impl(stream);
+}
+
 int accspmm_time_spmm(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp, const float* B,
                       float* C, uint32_t c_rows, uint32_t K, int32_t precision, int32_t warmup,
                       int32_t exe, float* avg_ms, void* stream) {

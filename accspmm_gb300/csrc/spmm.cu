@@ -154,7 +154,7 @@ __global__ void rwo_from_row_indices_kernel(const uint32_t* __restrict__ ri, uin
     for (uint32_t w = lo; w <= hi && w <= Weff; ++w) rwo[w] = t;
 }
 
-enum KernelKind { kDirect = 0, kPipe = 1 };
+enum KernelKind { kDirect = 0, kPipe = 1, kBulk = 2, kLean = 3 };
 
 struct Config {
     int kernel;
@@ -173,12 +173,17 @@ int env_int(const char* name, int dflt) {
 Config choose_config(uint32_t W, uint32_t K) {
     Config c;
     c.kernel = kDirect;
-    if (const char* e = std::getenv("ACCSPMM_KERNEL")) c.kernel = std::strcmp(e, "pipe") == 0 ? kPipe : kDirect;
+    if (const char* e = std::getenv("ACCSPMM_KERNEL"))
+        c.kernel = std::strcmp(e, "pipe") == 0   ? kPipe
+                   : std::strcmp(e, "bulk") == 0 ? kBulk
+                   : std::strcmp(e, "lean") == 0 ? kLean
+                                                 : kDirect;
     c.fs = K <= 32 ? 32 : 64;
     int fs = env_int("ACCSPMM_FS", 0);
     if (fs == 32 || fs == 64 || fs == 128) c.fs = fs;
     c.nw = env_int("ACCSPMM_NW", c.fs == 32 ? 8 : 4) == 4 ? 4 : 8;
     if (c.kernel == kPipe && c.fs >= 64) c.nw = 4;  // stage ring must fit in shared memory
+    if (c.kernel == kBulk) c.nw = env_int("ACCSPMM_NW", 4) == 2 ? 2 : 4;
     c.hints = env_int("ACCSPMM_HINTS", 1) ? 1 : 0;
     uint32_t slices = (K + c.fs - 1) / c.fs;
     // enough CTAs to fill every SM several times over, 4..32 windows each
@@ -238,6 +243,8 @@ int spmm_window_launch(const uint32_t* rwo, const uint32_t* tc_offset, const uin
                (K + uint32_t(cfg.fs) - 1) / uint32_t(cfg.fs), (W + cfg.wb - 1) / cfg.wb,
                cfg.slice_major};
     if (cfg.kernel == kPipe) return launch_pipe(a, cfg.fs, precision, cfg.nw, cfg.hints, s);
+    if (cfg.kernel == kBulk) return launch_bulk(a, cfg.fs, precision, cfg.nw, cfg.hints, s);
+    if (cfg.kernel == kLean) return launch_lean(a, cfg.fs, precision, env_int("ACCSPMM_MINB", 4), s);
     const bool x3 = precision == ACCSPMM_PREC_3XTF32;
     switch (cfg.fs) {
         case 32: return x3 ? launch_direct<32, ACCSPMM_PREC_3XTF32>(a, s) : launch_direct<32, ACCSPMM_PREC_TF32>(a, s);
@@ -285,6 +292,8 @@ int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uin
     return spmm_window_launch(rwo, ad->tc_offset, ad->tc_local_bit, ad->sparse_a2b, ad->data, Weff,
                               (ad->rows + kWin - 1) / kWin, ad->cols, B, C, K, precision, s);
 }
+
+int device_status_impl(void* stream) { return bulk_status(as_stream(stream), true); }
 
 int time_spmm_impl(const accspmm_metcf_t* m, const accspmm_adpbme_t* ad, const float* B, float* C,
                    uint32_t c_rows, uint32_t K, int precision, int warmup, int exe, float* avg_ms,

@@ -1,0 +1,327 @@
+// spmm_bulk.cu -- the SpMM kernel fed by bulk asynchronous copies (TMA).
+//
+// Same decomposition and arithmetic as the other SpMM kernels (a CTA per
+// window block and feature slice, equal per-warp tile pieces, partial windows
+// summed in warp order).  Each warp owns a ring of D shared-memory stages of U
+// tiles (B rows [U][8][FS] floats plus the tiles' bitmaps and value offsets)
+// with one mbarrier per stage.  For batch q + D - 1 the warp's lane 8u + k
+// issues one cp.async.bulk of row k of tile u -- min(FS, K - f0) floats of B
+// row sparseA2B[8t + 8u + k], or of a static zero row for padding -- and lane 0
+// posts the expected byte count; the warp then waits for batch q's barrier
+// and runs the MMAs from shared memory.  Gathers of 8U rows per instruction
+// keep up to (D - 1) U tiles of B in flight per warp without holding them in
+// registers.  Every wait is bounded: if a barrier does not complete within
+// the limit the kernel records ACCSPMM_ERROR_TIMEOUT in a device status word
+// (read by accspmm_device_status), stops consuming, waits (bounded) for its
+// own copies in flight and finishes normally.
+#include "common.hpp"
+#include "device_util.cuh"
+#include "spmm_common.cuh"
+
+namespace accspmm {
+
+// Zero source for the padding rows of a tile (FS <= 128 floats).
+static __device__ __align__(16) float g_zero_row[128] = {0.f};
+// Sticky status of bounded waits that expired (0 = none).
+static __device__ unsigned int g_bulk_status = 0;
+
+namespace {
+
+// A wait gives up after this long (the copies it waits for are a few KB of
+// valid global memory, normally landing within microseconds).
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+
+template <int FS>
+struct BulkCfg {
+    static constexpr int kU = FS >= 128 ? 2 : (FS == 64 ? 4 : 8);  // tiles per batch
+    static constexpr int kD = 4;                                    // stages per warp
+    static constexpr int kB = kU * 8 * FS;                          // floats of B per stage
+    static constexpr int kMeta = kU * 4;                            // (bits lo, hi, off, -) per tile
+    static constexpr int kStage = kB + kMeta;                       // floats per stage
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile(
+        "{\n\t.reg .b64 st;\n\t"
+        "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(bar),
+        "r"(bytes)
+        : "memory");
+}
+
+// One try_wait, suspending the thread for at most about 20 us.
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity), "r"(20000u)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait for a barrier phase, bounded by limit_ns of wall time; false if the
+// limit expired.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
+                                          uint64_t limit_ns = kWaitLimitNs) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (global_ns() - t0 > limit_ns) return false;
+    }
+}
+
+template <bool HINTS>
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar,
+                                          uint64_t pol) {
+    if constexpr (HINTS) {
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint "
+            "[%0], [%1], %2, [%3], %4;" ::"r"(dst),
+            "l"(src), "r"(bytes), "r"(bar), "l"(pol)
+            : "memory");
+    } else {
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+            "l"(src), "r"(bytes), "r"(bar)
+            : "memory");
+    }
+}
+
+template <int FS, int PREC, int NW, bool HINTS>
+__global__ void __launch_bounds__(NW * 32) spmm_bulk_kernel(const SpmmArgs a) {
+    constexpr int H = FS / 32;
+    using L = Layout<H>;
+    constexpr int NM = L::NM;
+    using Cf = BulkCfg<FS>;
+    constexpr int kU = Cf::kU, kD = Cf::kD;
+    constexpr int MA = (8 * kU + 31) / 32;
+    static_assert(8 * kU <= 64, "at most two a2b registers per lane");
+
+    extern __shared__ __align__(128) float smem[];
+    float* ring = smem;                                      // [NW][kD][kStage]
+    float* part = ring + size_t(NW) * kD * Cf::kStage;       // [2 NW][8][FS]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(part + 2 * NW * 8 * FS);  // [NW][kD]
+    uint32_t* s_rwo = reinterpret_cast<uint32_t*>(bars + NW * kD);
+
+    Block<FS, NW> blk;
+    blk.init(a, s_rwo, part);
+    const int lane = blk.lane, g = blk.g, tq = blk.tq;
+    const uint32_t tb = blk.bound(blk.warp), te = blk.bound(blk.warp + 1);
+
+    uint64_t pol_keep = 0;
+    if constexpr (HINTS) asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol_keep));
+
+    if (tb < te) {
+        float* my_ring = ring + size_t(blk.warp) * kD * Cf::kStage;
+        const uint32_t bar0 = smem_addr(bars + blk.warp * kD);
+        if (lane == 0) {
+            for (int d = 0; d < kD; ++d) mbar_init(bar0 + 8u * d, 1);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncwarp();
+
+        const uint32_t nb = (te - tb + kU - 1) / kU;
+        const uint32_t rowf = min(uint32_t(FS), a.K - blk.f0);  // floats copied per row
+        const uint32_t rowb = rowf * 4u;
+
+        // metadata of batch b: lane L holds a2b[8t + L] (+32), bits / offset of tile `lane`
+        uint32_t ma[MA];
+        uint64_t mb;
+        uint32_t mo;
+        auto load_meta = [&](uint32_t b) {
+            const uint32_t t = tb + b * kU;
+#pragma unroll
+            for (int j = 0; j < MA; ++j) {
+                const uint32_t e = 32 * j + lane;
+                ma[j] = (b < nb && e < 8 * kU && t + e / 8 < te) ? __ldg(a.a2b + size_t(t) * 8 + e) : kPad;
+            }
+            const uint32_t tl = t + uint32_t(lane);
+            const bool ok = b < nb && lane < kU && tl < te;
+            mb = ok ? __ldg(reinterpret_cast<const unsigned long long*>(a.bits) + tl) : 0ull;
+            mo = ok ? __ldg(a.tc_offset + tl) : 0u;
+        };
+
+        auto issue = [&](uint32_t b) {
+            if (b >= nb) return;
+            const uint32_t s = b % kD;
+            float* st = my_ring + size_t(s) * Cf::kStage;
+            const uint32_t t = tb + b * kU;
+            const uint32_t ntiles = min(uint32_t(kU), te - t);
+            const uint32_t bar = bar0 + 8u * s;
+            // the stage was last read by this warp's generic loads
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            if (lane == 0) mbar_expect_tx(bar, ntiles * 8u * rowb);
+            __syncwarp();
+#pragma unroll
+            for (int j = 0; j < MA; ++j) {
+                const uint32_t e = 32 * j + lane;  // (tile, row) = (e / 8, e % 8)
+                if (e < 8 * kU && e / 8 < ntiles) {
+                    const uint32_t idx = ma[j];
+                    const float* src = idx < a.cols ? a.B + size_t(idx) * a.K + blk.f0 : g_zero_row;
+                    bulk_copy<HINTS>(smem_addr(st + e * FS), src, rowb, bar, pol_keep);
+                }
+            }
+            if (lane < kU) {
+                uint32_t* sm = reinterpret_cast<uint32_t*>(st + Cf::kB) + 4 * lane;
+                sm[0] = uint32_t(mb);
+                sm[1] = uint32_t(mb >> 32);
+                sm[2] = mo;
+                if (uint32_t(lane) < ntiles) asm volatile("prefetch.global.L1 [%0];" ::"l"(a.vals + mo));
+            }
+        };
+
+        BitDecode dec;
+        dec.init(g, tq);
+        uint32_t wl = blk.window_of(tb);
+        uint32_t next_bound = blk.s_rwo[wl + 1];
+        bool first_win = true;
+        bool failed = false;
+        uint32_t fail_q = 0;
+        float acc[NM][4];
+#pragma unroll
+        for (int m = 0; m < NM; ++m) acc[m][0] = acc[m][1] = acc[m][2] = acc[m][3] = 0.f;
+
+        // prologue: batches 0 .. kD-2 in flight
+        for (int d = 0; d < kD - 1; ++d) {
+            load_meta(uint32_t(d));
+            issue(uint32_t(d));
+        }
+        load_meta(kD - 1);
+        for (uint32_t q = 0; q < nb && !failed; ++q) {
+            issue(q + kD - 1);
+            load_meta(q + kD);
+            const uint32_t s = q % kD;
+            const bool landed = mbar_wait(bar0 + 8u * s, (q / kD) & 1u);
+            if (!__all_sync(0xffffffffu, landed)) {  // warp-uniform outcome
+                failed = true;
+                fail_q = q;
+                break;
+            }
+            __syncwarp();
+            const float* st = my_ring + size_t(s) * Cf::kStage;
+            const uint32_t* sm = reinterpret_cast<const uint32_t*>(st + Cf::kB);
+            const uint32_t t = tb + q * kU;
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                const uint32_t tt = t + u;
+                if (tt >= te) break;
+                if (tt >= next_bound) {
+                    blk.flush(a, acc, wl, tb, te, first_win);
+                    first_win = false;
+#pragma unroll
+                    for (int mm = 0; mm < NM; ++mm) acc[mm][0] = acc[mm][1] = acc[mm][2] = acc[mm][3] = 0.f;
+                    while (blk.s_rwo[wl + 1] <= tt) ++wl;
+                    next_bound = blk.s_rwo[wl + 1];
+                }
+                const uint64_t bm = uint64_t(sm[4 * u]) | (uint64_t(sm[4 * u + 1]) << 32);
+                const uint32_t to = sm[4 * u + 2];
+                uint32_t x0, x1;
+                bool q0, q1;
+                dec.decode(bm, x0, x1, q0, q1);
+                const float av0 = q0 ? __ldg(a.vals + to + x0) : 0.f;
+                const float av1 = q1 ? __ldg(a.vals + to + x1) : 0.f;
+                float4 r0[H], r1[H];
+                const float* sb = st + u * 8 * FS + 4 * g;
+#pragma unroll
+                for (int h = 0; h < H; ++h) {
+                    r0[h] = *reinterpret_cast<const float4*>(sb + tq * FS + 32 * h);
+                    r1[h] = *reinterpret_cast<const float4*>(sb + (tq + 4) * FS + 32 * h);
+                }
+                tile_mma<H, PREC>(acc, r0, r1, av0, av1);
+            }
+            __syncwarp();
+        }
+        if (failed) {
+            if (lane == 0) atomicOr(&g_bulk_status, 1u);
+            // batches fail_q .. fail_q + kD - 1 may still have copies in
+            // flight into this warp's ring: let them land (bounded) first
+            for (uint32_t b = fail_q; b < nb && b < fail_q + kD; ++b)
+                mbar_wait(bar0 + 8u * (b % kD), (b / kD) & 1u);
+        } else {
+            blk.flush(a, acc, wl, tb, te, first_win);
+        }
+    }
+    __syncthreads();
+    blk.finish(a);
+}
+
+template <int FS, int NW>
+size_t bulk_smem(uint32_t wb) {
+    using Cf = BulkCfg<FS>;
+    return (size_t(NW) * Cf::kD * Cf::kStage + size_t(2 * NW * 8 * FS)) * 4 + size_t(NW) * Cf::kD * 8 +
+           size_t(wb + 1) * 4;
+}
+
+template <int FS, int PREC, int NW, bool HINTS>
+int launch_one(const SpmmArgs& a, cudaStream_t s) {
+    const size_t smem = bulk_smem<FS, NW>(a.wb);
+    if (smem > 227 * 1024) ACC_FAIL(ACCSPMM_ERROR_UNSUPPORTED, "shared memory %zu too large", smem);
+    static unsigned attr_set = 0;  // one bit per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 32 && !(attr_set & (1u << dev))) {
+        ACC_CUDA(cudaFuncSetAttribute(spmm_bulk_kernel<FS, PREC, NW, HINTS>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+        attr_set |= 1u << dev;
+    }
+    const uint64_t grid = uint64_t(a.n_wblocks) * a.n_slices;
+    if (grid == 0) return ACCSPMM_SUCCESS;
+    if (grid > 0x7FFFFFFFull) ACC_FAIL(ACCSPMM_ERROR_OVERFLOW, "grid too large");
+    spmm_bulk_kernel<FS, PREC, NW, HINTS><<<unsigned(grid), NW * 32, smem, s>>>(a);
+    ACC_LAUNCH_CHECK();
+    return ACCSPMM_SUCCESS;
+}
+
+template <int FS, int PREC>
+int launch_nw(const SpmmArgs& a, int nw, int hints, cudaStream_t s) {
+    if (nw == 4) return hints ? launch_one<FS, PREC, 4, true>(a, s) : launch_one<FS, PREC, 4, false>(a, s);
+    return hints ? launch_one<FS, PREC, 2, true>(a, s) : launch_one<FS, PREC, 2, false>(a, s);
+}
+
+template <int PREC>
+int launch_prec(const SpmmArgs& a, int fs, int nw, int hints, cudaStream_t s) {
+    switch (fs) {
+        case 32: return launch_nw<32, PREC>(a, nw, hints, s);
+        case 64: return launch_nw<64, PREC>(a, nw, hints, s);
+        default: return launch_nw<128, PREC>(a, nw, hints, s);
+    }
+}
+
+}  // namespace
+
+int launch_bulk(const SpmmArgs& a, int fs, int precision, int nw, int hints, cudaStream_t s) {
+    if (a.K % 4) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "K must be a multiple of 4");
+    return precision == ACCSPMM_PREC_3XTF32 ? launch_prec<ACCSPMM_PREC_3XTF32>(a, fs, nw, hints, s)
+                                            : launch_prec<ACCSPMM_PREC_TF32>(a, fs, nw, hints, s);
+}
+
+int bulk_status(cudaStream_t s, bool clear) {
+    ACC_CUDA(cudaStreamSynchronize(s));
+    unsigned int v = 0;
+    ACC_CUDA(cudaMemcpyFromSymbol(&v, g_bulk_status, sizeof v));
+    if (v && clear) {
+        unsigned int z = 0;
+        ACC_CUDA(cudaMemcpyToSymbol(g_bulk_status, &z, sizeof z));
+    }
+    if (v) ACC_FAIL(ACCSPMM_ERROR_TIMEOUT, "a bounded wait in the SpMM kernel expired");
+    return ACCSPMM_SUCCESS;
+}
+
+}  // namespace accspmm

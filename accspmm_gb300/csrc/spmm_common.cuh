@@ -313,5 +313,10 @@ struct Block {
 // Launch of the cp.async-pipelined kernel (spmm_pipe.cu).
 int launch_pipe(const SpmmArgs& a, int fs, int precision, int nw, int hints, cudaStream_t s);
 size_t pipe_smem_bytes(int fs, int nw, uint32_t wb);
+// Launch of the bulk-copy (TMA) kernel and its status word (spmm_bulk.cu).
+int launch_bulk(const SpmmArgs& a, int fs, int precision, int nw, int hints, cudaStream_t s);
+int bulk_status(cudaStream_t s, bool clear);
+// Launch of the occupancy-sized register-direct kernel (spmm_lean.cu).
+int launch_lean(const SpmmArgs& a, int fs, int precision, int minb, cudaStream_t s);
 
 }  // namespace accspmm

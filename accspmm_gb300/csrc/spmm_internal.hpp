@@ -22,6 +22,7 @@ int spmm_tf32_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t 
                    void* stream);
 int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uint32_t c_rows,
                        uint32_t K, int precision, void* stream);
+int device_status_impl(void* stream);
 int time_spmm_impl(const accspmm_metcf_t* m, const accspmm_adpbme_t* ad, const float* B, float* C,
                    uint32_t c_rows, uint32_t K, int precision, int warmup, int exe, float* avg_ms,
                    void* stream);

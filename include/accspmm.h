@@ -214,6 +214,13 @@ int accspmm_time_spmm(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp,
                       int32_t precision, int32_t warmup, int32_t exe,
                       float* avg_ms, void* stream);
 
+/* Synchronises `stream`, then reports (and clears) the sticky status of the
+ * SpMM kernels' bounded waits on the current device: ACCSPMM_ERROR_TIMEOUT if
+ * a wait on an asynchronous copy expired since the last call (the affected
+ * output rows are then undefined), else ACCSPMM_SUCCESS.  No counterpart in
+ * the reference, whose kernels have no asynchronous-copy waits. */
+int accspmm_device_status(void* stream);
+
 #ifdef __cplusplus
 }
 #endif
