@@ -86,6 +86,8 @@ _SIGS = {
     "accspmm_spmm_tf32": ([C.POINTER(METCF), vp, vp, u32, i32, vp], C.c_int),
     "accspmm_spmm_adaptive": ([C.POINTER(ADPBME), vp, vp, u32, u32, i32, vp], C.c_int),
     "accspmm_device_status": ([vp], C.c_int),
+    "accspmm_spmm_adaptive_noalloc": ([C.POINTER(ADPBME), vp, vp, u32, u32, i32, vp], C.c_int),
+    "accspmm_noalloc_max_c_rows": ([], C.c_uint32),
     "accspmm_time_spmm": ([C.POINTER(METCF), C.POINTER(ADPBME), vp, vp, u32, u32, i32, i32, i32,
                            f32p, vp], C.c_int),
 }

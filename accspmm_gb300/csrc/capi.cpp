@@ -316,6 +316,14 @@ int accspmm_spmm_adaptive(const accspmm_adpbme_t* adp, const float* B, float* C,
     return spmm_adaptive_impl(adp, B, C, c_rows, K, precision, stream);
 }
 
+int accspmm_spmm_adaptive_noalloc(const accspmm_adpbme_t* adp, const float* B, float* C,
+                                  uint32_t c_rows, uint32_t K, int32_t precision, void* stream) {
+    clear_error();
+    return spmm_adaptive_noalloc_impl(adp, B, C, c_rows, K, precision, stream);
+}
+
+uint32_t accspmm_noalloc_max_c_rows(void) { return noalloc_max_c_rows(); }
+
 int accspmm_device_status(void* stream) {
     clear_error();
     return device_status_impl(stream);

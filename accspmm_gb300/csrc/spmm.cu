@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 
 #include "common.hpp"
 #include "device_util.cuh"
@@ -286,6 +287,67 @@ int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uin
     ACC_CUDA(scratch.alloc(size_t(Weff) + 2, s));
     uint32_t* rwo = scratch.p;
     uint32_t* err = scratch.p + Weff + 1;
+    ACC_CUDA(cudaMemsetAsync(err, 0, 4, s));
+    rwo_from_row_indices_kernel<<<(T + 1 + 255) / 256, 256, 0, s>>>(ad->row_indices, T, Weff, rwo, err);
+    ACC_LAUNCH_CHECK();
+    return spmm_window_launch(rwo, ad->tc_offset, ad->tc_local_bit, ad->sparse_a2b, ad->data, Weff,
+                              (ad->rows + kWin - 1) / kWin, ad->cols, B, C, K, precision, s);
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free adaptive SpMM.  Callers that may not allocate device memory
+// -- code running while a CUDA graph is being captured into a pool they do
+// not own, real-time loops that forbid allocator calls, hosts whose memory
+// budget is fixed up front -- use this variant: its only scratch (the
+// rowWindowOffset derived from rowIndices plus a status word) lives in the
+// file-scope array below, which every GPU that loads the library holds until
+// the process exits.  All calls share the array, so calls that overlap on the
+// GPU (different streams, no ordering between them) race on it.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kNoAllocWords = 1u << 20;  // 4 MiB: windows + 2 words
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocWords];
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device (the host-side symbol is not a device address).
+static int noalloc_scratch(uint32_t** out) {
+    static std::mutex mu;
+    static uint32_t* ptr[64] = {nullptr};
+    int dev = 0;
+    ACC_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) ACC_FAIL(ACCSPMM_ERROR_UNSUPPORTED, "device %d out of range", dev);
+    std::lock_guard<std::mutex> lock(mu);
+    if (!ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            ACC_FAIL(ACCSPMM_ERROR_CUDA, "cudaGetSymbolAddress of the no-alloc scratch failed: %s",
+                     cudaGetErrorString(e));
+        ptr[dev] = static_cast<uint32_t*>(p);
+    }
+    *out = ptr[dev];
+    return ACCSPMM_SUCCESS;
+}
+
+uint32_t noalloc_max_c_rows() { return (kNoAllocWords - 2) * kWin; }
+
+int spmm_adaptive_noalloc_impl(const accspmm_adpbme_t* ad, const float* B, float* C,
+                               uint32_t c_rows, uint32_t K, int precision, void* stream) {
+    if (!ad || ad->space != ACCSPMM_DEVICE) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "AdpBME must be on the device");
+    int st = check_dense(B, C, K, precision);
+    if (st) return st;
+    if (c_rows % kWin) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "c_rows=%u must be a multiple of 8", c_rows);
+    if (c_rows > noalloc_max_c_rows())
+        ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE,
+                 "c_rows=%u exceeds the allocation-free maximum of %u rows; use accspmm_spmm_adaptive",
+                 c_rows, noalloc_max_c_rows());
+    cudaStream_t s = as_stream(stream);
+    const uint32_t Weff = c_rows / kWin, T = ad->num_tiles;
+    if (Weff == 0) return ACCSPMM_SUCCESS;
+    uint32_t* scratch = nullptr;
+    st = noalloc_scratch(&scratch);
+    if (st) return st;
+    uint32_t* rwo = scratch;             // [Weff + 1], fully rewritten below
+    uint32_t* err = scratch + Weff + 1;  // must start at zero
     ACC_CUDA(cudaMemsetAsync(err, 0, 4, s));
     rwo_from_row_indices_kernel<<<(T + 1 + 255) / 256, 256, 0, s>>>(ad->row_indices, T, Weff, rwo, err);
     ACC_LAUNCH_CHECK();

@@ -23,6 +23,9 @@ int spmm_tf32_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t 
 int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uint32_t c_rows,
                        uint32_t K, int precision, void* stream);
 int device_status_impl(void* stream);
+int spmm_adaptive_noalloc_impl(const accspmm_adpbme_t* ad, const float* B, float* C,
+                               uint32_t c_rows, uint32_t K, int precision, void* stream);
+uint32_t noalloc_max_c_rows();
 int time_spmm_impl(const accspmm_metcf_t* m, const accspmm_adpbme_t* ad, const float* B, float* C,
                    uint32_t c_rows, uint32_t K, int precision, int warmup, int exe, float* avg_ms,
                    void* stream);

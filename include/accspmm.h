@@ -206,6 +206,26 @@ int accspmm_spmm_adaptive(const accspmm_adpbme_t* adp, const float* B,
                           float* C, uint32_t c_rows, uint32_t K,
                           int32_t precision, void* stream);
 
+/* Allocation-free variant of accspmm_spmm_adaptive, for callers that cannot
+ * allocate device memory at call time: work issued while a CUDA graph is
+ * captured into a memory pool the caller does not own, real-time loops that
+ * forbid allocator calls, or hosts whose device memory is budgeted up front.
+ * No counterpart in the reference.  It calls no cudaMalloc, cudaFree or other
+ * allocating routine: its scratch (the row-window offsets derived from
+ * rowIndices, 4 (c_rows / 8 + 2) bytes) lives in a 4 MiB array compiled into
+ * the library, which every GPU that loads the library holds until the
+ * process exits.  c_rows may be at most accspmm_noalloc_max_c_rows()
+ * (8,388,592); larger sizes return ACCSPMM_ERROR_INVALID_VALUE.  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * and caches it; make that first call before any stream capture.  Every call
+ * shares the one array and leaves the last call's contents in it, so calls
+ * that overlap on the GPU (unordered streams) race; order them on one stream
+ * or with events.  Same inputs, outputs and results as accspmm_spmm_adaptive. */
+int accspmm_spmm_adaptive_noalloc(const accspmm_adpbme_t* adp, const float* B,
+                                  float* C, uint32_t c_rows, uint32_t K,
+                                  int32_t precision, void* stream);
+uint32_t accspmm_noalloc_max_c_rows(void);
+
 /* The timing loop of TF32Compute::executeKernel, include/tf32_comp.hpp:33-46:
  * `warmup` untimed launches, then `exe` launches between two CUDA events on
  * `stream`; *avg_ms = elapsed / exe.  `adp` may be NULL (plain path). */
