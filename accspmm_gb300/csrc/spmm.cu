@@ -37,6 +37,9 @@ namespace {
 
 constexpr int kNW = 8;  // warps per CTA of the register-direct kernel
 
+// Zero source for the padding rows of a tile (FS <= 128 floats).
+__device__ __align__(16) float g_zero_row_direct[128] = {0.f};
+
 __device__ __forceinline__ uint64_t shfl_u64(uint64_t v, int src) {
     uint32_t lo = __shfl_sync(0xffffffffu, uint32_t(v), src);
     uint32_t hi = __shfl_sync(0xffffffffu, uint32_t(v >> 32), src);
@@ -138,24 +141,165 @@ __global__ void __launch_bounds__(kNW * 32, 2) spmm_window_kernel(const SpmmArgs
     blk.finish(a);
 }
 
-// rwo[w] = first tile whose window (row_indices / 8) is >= w, for w in
-// [0, Weff]; tiles claiming windows >= Weff raise *err.
+// Double-buffered register-direct kernel: the gathers of batch q + 1 are
+// issued before the MMAs of batch q, so every warp keeps a batch of B rows
+// in flight while it computes instead of alternating load and compute phases.
+template <int FS, int PREC, int U>
+__global__ void __launch_bounds__(kNW * 32, 2) spmm_db_kernel(const SpmmArgs a) {
+    constexpr int H = FS / 32;
+    using L = Layout<H>;
+    constexpr int NM = L::NM;
+    constexpr int MA = (8 * U + 31) / 32;
+
+    extern __shared__ __align__(16) float smem[];
+    float* part = smem;
+    uint32_t* s_rwo = reinterpret_cast<uint32_t*>(smem + 2 * kNW * 8 * FS);
+    Block<FS, kNW> blk;
+    blk.init(a, s_rwo, part);
+    const int lane = blk.lane, g = blk.g, tq = blk.tq;
+    const uint32_t tb = blk.bound(blk.warp), te = blk.bound(blk.warp + 1);
+
+    if (tb < te) {
+        uint32_t wl = blk.window_of(tb);
+        uint32_t next_bound = blk.s_rwo[wl + 1];
+        bool first_win = true;
+        float acc[NM][4];
+#pragma unroll
+        for (int m = 0; m < NM; ++m) acc[m][0] = acc[m][1] = acc[m][2] = acc[m][3] = 0.f;
+
+        uint32_t ma[MA];
+        uint64_t mb;
+        uint32_t mo;
+        auto load_meta = [&](uint32_t t) {
+#pragma unroll
+            for (int j = 0; j < MA; ++j) {
+                uint32_t e = 32 * j + lane;
+                ma[j] = (e < 8 * U && t + e / 8 < te) ? __ldg(a.a2b + size_t(t) * 8 + e) : kPad;
+            }
+            uint32_t tl = t + uint32_t(lane);
+            bool ok = lane < U && tl < te;
+            mb = ok ? __ldg(reinterpret_cast<const unsigned long long*>(a.bits) + tl) : 0ull;
+            mo = ok ? __ldg(a.tc_offset + tl) : 0u;
+        };
+
+        BitDecode dec;
+        dec.init(g, tq);
+        // lane offsets inside a row slice, clamped to the row; padding reads
+        // a zero row
+        const uint32_t kr = a.K - blk.f0;
+        uint32_t off[H];
+#pragma unroll
+        for (int h = 0; h < H; ++h) off[h] = min(uint32_t(32 * h + 4 * g), kr - 4);
+        const float* Bs = a.B + blk.f0;
+
+        struct Batch {
+            float4 r0[U][H], r1[U][H];
+            float av0[U], av1[U];
+        };
+        auto gather = [&](Batch& bt) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint32_t i0 = __shfl_sync(0xffffffffu, ma[(8 * u) / 32], (8 * u + tq) & 31);
+                const uint32_t i1 = __shfl_sync(0xffffffffu, ma[(8 * u) / 32], (8 * u + tq + 4) & 31);
+                const float* p0 = i0 < a.cols ? Bs + size_t(i0) * a.K : g_zero_row_direct;
+                const float* p1 = i1 < a.cols ? Bs + size_t(i1) * a.K : g_zero_row_direct;
+#pragma unroll
+                for (int h = 0; h < H; ++h) {
+                    bt.r0[u][h] = ldg_f4_ordered(p0 + off[h]);
+                    bt.r1[u][h] = ldg_f4_ordered(p1 + off[h]);
+                }
+                const uint64_t bm = shfl_u64(mb, u);
+                const uint32_t to = __shfl_sync(0xffffffffu, mo, u);
+                uint32_t x0, x1;
+                bool q0, q1;
+                dec.decode(bm, x0, x1, q0, q1);
+                bt.av0[u] = q0 ? ldg_f32_ordered(a.vals + to + x0) : 0.f;
+                bt.av1[u] = q1 ? ldg_f32_ordered(a.vals + to + x1) : 0.f;
+            }
+        };
+        auto compute = [&](uint32_t t, const Batch& bt) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint32_t tt = t + u;
+                if (tt >= te) break;
+                if (tt >= next_bound) {
+                    blk.flush(a, acc, wl, tb, te, first_win);
+                    first_win = false;
+#pragma unroll
+                    for (int m = 0; m < NM; ++m) acc[m][0] = acc[m][1] = acc[m][2] = acc[m][3] = 0.f;
+                    while (blk.s_rwo[wl + 1] <= tt) ++wl;
+                    next_bound = blk.s_rwo[wl + 1];
+                }
+                tile_mma<H, PREC>(acc, bt.r0[u], bt.r1[u], bt.av0[u], bt.av1[u]);
+            }
+        };
+
+        Batch b0, b1;
+        load_meta(tb);
+        gather(b0);
+        if (tb + U < te) load_meta(tb + U);
+        for (uint32_t t = tb; t < te; t += 2 * U) {
+            // b0 holds batch t, the metadata registers batch t + U
+            if (t + U < te) {
+                gather(b1);
+                if (t + 2 * U < te) load_meta(t + 2 * U);
+            }
+            compute(t, b0);
+            if (t + U >= te) break;
+            // b1 holds batch t + U, the metadata registers batch t + 2U
+            if (t + 2 * U < te) {
+                gather(b0);
+                if (t + 3 * U < te) load_meta(t + 3 * U);
+            }
+            compute(t + U, b1);
+        }
+        blk.flush(a, acc, wl, tb, te, first_win);
+    }
+    __syncthreads();
+    blk.finish(a);
+}
+
+template <int FS, int PREC, int U>
+int launch_db(const SpmmArgs& a, cudaStream_t s) {
+    const size_t smem = size_t(2 * kNW * 8 * FS) * 4 + size_t(a.wb + 1) * 4;
+    static unsigned attr_set = 0;  // one bit per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 32 && !(attr_set & (1u << dev))) {
+        ACC_CUDA(cudaFuncSetAttribute(spmm_db_kernel<FS, PREC, U>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+        attr_set |= 1u << dev;
+    }
+    const uint64_t grid = uint64_t(a.n_wblocks) * a.n_slices;
+    if (grid == 0) return ACCSPMM_SUCCESS;
+    if (grid > 0x7FFFFFFFull) ACC_FAIL(ACCSPMM_ERROR_OVERFLOW, "grid too large");
+    spmm_db_kernel<FS, PREC, U><<<unsigned(grid), kNW * 32, smem, s>>>(a);
+    ACC_LAUNCH_CHECK();
+    return ACCSPMM_SUCCESS;
+}
+
+// rwo[w] = first tile whose window start row (row_indices, non-decreasing)
+// is >= 8w, for w in [0, Weff]: one thread per window, binary search over the
+// tiles.  Tiles that claim windows >= Weff, or a decreasing row_indices, raise
+// *err.
 __global__ void rwo_from_row_indices_kernel(const uint32_t* __restrict__ ri, uint32_t T,
                                             uint32_t Weff, uint32_t* __restrict__ rwo,
                                             uint32_t* __restrict__ err) {
-    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t > T) return;
-    uint32_t lo = t == 0 ? 0u : ri[t - 1] / kWin + 1;
-    uint32_t hi = t == T ? Weff : ri[t] / kWin;
-    if (t < T && hi >= Weff) {
-        atomicOr(err, 1u);
-        hi = Weff;
+    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w > Weff) return;
+    const uint64_t row = uint64_t(w) * kWin;
+    uint32_t lo = 0, hi = T;
+    while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if (uint64_t(ri[mid]) < row) lo = mid + 1;
+        else hi = mid;
     }
-    if (t > 0 && t < T && ri[t] < ri[t - 1]) atomicOr(err, 2u);
-    for (uint32_t w = lo; w <= hi && w <= Weff; ++w) rwo[w] = t;
+    rwo[w] = lo;
+    if (w == Weff && lo < T) atomicOr(err, 1u);
+    if (w < Weff && lo < T && lo > 0 && ri[lo] < ri[lo - 1]) atomicOr(err, 2u);
 }
 
-enum KernelKind { kDirect = 0, kPipe = 1, kBulk = 2, kLean = 3 };
+enum KernelKind { kDirect = 0, kPipe = 1, kBulk = 2, kLean = 3, kDb = 4 };
 
 struct Config {
     int kernel;
@@ -171,6 +315,11 @@ int env_int(const char* name, int dflt) {
     return e && *e ? std::atoi(e) : dflt;
 }
 
+// Launch shape from (W, K).  Measured on GB300 with the 1M-row power-law
+// workload: 128-column slices (the whole row of B for K <= 128) and 16
+// windows per CTA are fastest for K >= 128; narrower K uses a slice of K.
+// Every field can be overridden through the environment for tuning
+// (ACCSPMM_KERNEL, _FS, _WB, _NW, _ORDER, _HINTS).
 Config choose_config(uint32_t W, uint32_t K) {
     Config c;
     c.kernel = kDirect;
@@ -178,8 +327,9 @@ Config choose_config(uint32_t W, uint32_t K) {
         c.kernel = std::strcmp(e, "pipe") == 0   ? kPipe
                    : std::strcmp(e, "bulk") == 0 ? kBulk
                    : std::strcmp(e, "lean") == 0 ? kLean
+                   : std::strcmp(e, "db") == 0   ? kDb
                                                  : kDirect;
-    c.fs = K <= 32 ? 32 : 64;
+    c.fs = K <= 32 ? 32 : K <= 64 ? 64 : 128;
     int fs = env_int("ACCSPMM_FS", 0);
     if (fs == 32 || fs == 64 || fs == 128) c.fs = fs;
     c.nw = env_int("ACCSPMM_NW", c.fs == 32 ? 8 : 4) == 4 ? 4 : 8;
@@ -187,10 +337,10 @@ Config choose_config(uint32_t W, uint32_t K) {
     if (c.kernel == kBulk) c.nw = env_int("ACCSPMM_NW", 4) == 2 ? 2 : 4;
     c.hints = env_int("ACCSPMM_HINTS", 1) ? 1 : 0;
     uint32_t slices = (K + c.fs - 1) / c.fs;
-    // enough CTAs to fill every SM several times over, 4..32 windows each
-    uint64_t want = uint64_t(sm_count()) * 16;
-    uint64_t wb = (uint64_t(W) * slices + want - 1) / want;
-    c.wb = uint32_t(std::min<uint64_t>(32, std::max<uint64_t>(4, wb)));
+    // 16 windows per CTA, fewer for small matrices so that every SM gets work
+    uint64_t want = uint64_t(sm_count()) * 4;
+    uint64_t wb = std::max<uint64_t>(1, (uint64_t(W) * slices) / want);
+    c.wb = uint32_t(std::min<uint64_t>(16, std::max<uint64_t>(2, wb)));
     int wbe = env_int("ACCSPMM_WB", 0);
     if (wbe >= 1 && wbe <= 1024) c.wb = uint32_t(wbe);
     c.slice_major = 0;
@@ -246,6 +396,17 @@ int spmm_window_launch(const uint32_t* rwo, const uint32_t* tc_offset, const uin
     if (cfg.kernel == kPipe) return launch_pipe(a, cfg.fs, precision, cfg.nw, cfg.hints, s);
     if (cfg.kernel == kBulk) return launch_bulk(a, cfg.fs, precision, cfg.nw, cfg.hints, s);
     if (cfg.kernel == kLean) return launch_lean(a, cfg.fs, precision, env_int("ACCSPMM_MINB", 4), s);
+    if (cfg.kernel == kDb) {
+        const bool x3 = precision == ACCSPMM_PREC_3XTF32;
+        const int u = env_int("ACCSPMM_U", 0);
+        switch (cfg.fs) {
+            case 32: return x3 ? launch_db<32, ACCSPMM_PREC_3XTF32, 4>(a, s) : launch_db<32, ACCSPMM_PREC_TF32, 4>(a, s);
+            case 64:
+                if (u == 1) return x3 ? launch_db<64, ACCSPMM_PREC_3XTF32, 1>(a, s) : launch_db<64, ACCSPMM_PREC_TF32, 1>(a, s);
+                return x3 ? launch_db<64, ACCSPMM_PREC_3XTF32, 2>(a, s) : launch_db<64, ACCSPMM_PREC_TF32, 2>(a, s);
+            default: return x3 ? launch_db<128, ACCSPMM_PREC_3XTF32, 1>(a, s) : launch_db<128, ACCSPMM_PREC_TF32, 1>(a, s);
+        }
+    }
     const bool x3 = precision == ACCSPMM_PREC_3XTF32;
     switch (cfg.fs) {
         case 32: return x3 ? launch_direct<32, ACCSPMM_PREC_3XTF32>(a, s) : launch_direct<32, ACCSPMM_PREC_TF32>(a, s);
@@ -288,7 +449,7 @@ int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uin
     uint32_t* rwo = scratch.p;
     uint32_t* err = scratch.p + Weff + 1;
     ACC_CUDA(cudaMemsetAsync(err, 0, 4, s));
-    rwo_from_row_indices_kernel<<<(T + 1 + 255) / 256, 256, 0, s>>>(ad->row_indices, T, Weff, rwo, err);
+    rwo_from_row_indices_kernel<<<(Weff + 1 + 255) / 256, 256, 0, s>>>(ad->row_indices, T, Weff, rwo, err);
     ACC_LAUNCH_CHECK();
     return spmm_window_launch(rwo, ad->tc_offset, ad->tc_local_bit, ad->sparse_a2b, ad->data, Weff,
                               (ad->rows + kWin - 1) / kWin, ad->cols, B, C, K, precision, s);
@@ -349,7 +510,7 @@ int spmm_adaptive_noalloc_impl(const accspmm_adpbme_t* ad, const float* B, float
     uint32_t* rwo = scratch;             // [Weff + 1], fully rewritten below
     uint32_t* err = scratch + Weff + 1;  // must start at zero
     ACC_CUDA(cudaMemsetAsync(err, 0, 4, s));
-    rwo_from_row_indices_kernel<<<(T + 1 + 255) / 256, 256, 0, s>>>(ad->row_indices, T, Weff, rwo, err);
+    rwo_from_row_indices_kernel<<<(Weff + 1 + 255) / 256, 256, 0, s>>>(ad->row_indices, T, Weff, rwo, err);
     ACC_LAUNCH_CHECK();
     return spmm_window_launch(rwo, ad->tc_offset, ad->tc_local_bit, ad->sparse_a2b, ad->data, Weff,
                               (ad->rows + kWin - 1) / kWin, ad->cols, B, C, K, precision, s);
