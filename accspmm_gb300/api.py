@@ -270,6 +270,50 @@ class DeviceADPBME(DeviceObject):
              c_rows, K, precision, _stream(stream))
 
 
+class Batch:
+    """A batch plan: many device METCF matrices in one persistent launch.
+
+    items: list of (DeviceMETCF, B, C, K); B and C must stay allocated and in
+    place for the plan's lifetime."""
+
+    def __init__(self, items, precision=capi.PREC_TF32):
+        arr = (capi.BATCHITEM * len(items))()
+        for i, (m, B, C_out, K) in enumerate(items):
+            arr[i].metcf = C.pointer(m.struct)
+            arr[i].B = C.c_void_p(_addr(B))
+            arr[i].C = C.c_void_p(_addr(C_out))
+            arr[i].K = K
+        self._keep = [it[0] for it in items]
+        h = C.c_void_p()
+        call("accspmm_batch_create", arr, len(items), precision, C.byref(h))
+        self.h = h
+
+    def run(self, stream=None):
+        call("accspmm_batch_run", self.h, _stream(stream))
+
+    def capture(self, stream):
+        call("accspmm_batch_capture", self.h, _stream(stream))
+
+    def launch_graph(self, stream):
+        call("accspmm_batch_launch_graph", self.h, _stream(stream))
+
+    def info(self):
+        n, w, fs = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        call("accspmm_batch_info", self.h, C.byref(n), C.byref(w), C.byref(fs))
+        return n.value, w.value, fs.value
+
+    def destroy(self):
+        if self.h:
+            load().accspmm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
 def time_spmm(metcf: DeviceMETCF | None, adp: DeviceADPBME | None, B, C_out, c_rows: int, K: int,
               precision=capi.PREC_TF32, warmup=10, exe=10, stream=None) -> float:
     """TF32Compute's timing loop (include/tf32_comp.hpp:33-46): average ms."""

@@ -65,6 +65,10 @@ class ADPBME(C.Structure):
                 ("data", f32p), ("space", i32), ("owned", i32)]
 
 
+class BATCHITEM(C.Structure):
+    _fields_ = [("metcf", C.POINTER(METCF)), ("B", vp), ("C", vp), ("K", u32)]
+
+
 _SIGS = {
     "accspmm_version": ([], C.c_char_p),
     "accspmm_last_error": ([], C.c_char_p),
@@ -86,6 +90,12 @@ _SIGS = {
     "accspmm_spmm_tf32": ([C.POINTER(METCF), vp, vp, u32, i32, vp], C.c_int),
     "accspmm_spmm_adaptive": ([C.POINTER(ADPBME), vp, vp, u32, u32, i32, vp], C.c_int),
     "accspmm_device_status": ([vp], C.c_int),
+    "accspmm_batch_create": ([C.POINTER(BATCHITEM), u32, i32, C.POINTER(vp)], C.c_int),
+    "accspmm_batch_run": ([vp, vp], C.c_int),
+    "accspmm_batch_capture": ([vp, vp], C.c_int),
+    "accspmm_batch_launch_graph": ([vp, vp], C.c_int),
+    "accspmm_batch_info": ([vp, u32p, u32p, u32p], C.c_int),
+    "accspmm_batch_destroy": ([vp], None),
     "accspmm_spmm_adaptive_noalloc": ([C.POINTER(ADPBME), vp, vp, u32, u32, i32, vp], C.c_int),
     "accspmm_noalloc_max_c_rows": ([], C.c_uint32),
     "accspmm_time_spmm": ([C.POINTER(METCF), C.POINTER(ADPBME), vp, vp, u32, u32, i32, i32, i32,

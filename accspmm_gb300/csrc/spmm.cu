@@ -29,116 +29,28 @@
 #include "common.hpp"
 #include "device_util.cuh"
 #include "spmm_common.cuh"
+#include "spmm_direct.cuh"
 #include "spmm_internal.hpp"
 
 namespace accspmm {
 
 namespace {
 
-constexpr int kNW = 8;  // warps per CTA of the register-direct kernel
+constexpr int kNW = kDirectNW;  // warps per CTA of the register-direct kernels
 
 // Zero source for the padding rows of a tile (FS <= 128 floats).
 __device__ __align__(16) float g_zero_row_direct[128] = {0.f};
 
-__device__ __forceinline__ uint64_t shfl_u64(uint64_t v, int src) {
-    uint32_t lo = __shfl_sync(0xffffffffu, uint32_t(v), src);
-    uint32_t hi = __shfl_sync(0xffffffffu, uint32_t(v >> 32), src);
-    return (uint64_t(hi) << 32) | lo;
-}
 
-// Register-direct kernel: each lane loads its B fragments straight from
-// global memory, a batch of U tiles at a time.
+// One-matrix launch of the register-direct kernel: one CTA per work item.
 template <int FS, int PREC>
 __global__ void __launch_bounds__(kNW * 32, 2) spmm_window_kernel(const SpmmArgs a) {
-    constexpr int H = FS / 32;
-    using L = Layout<H>;
-    constexpr int NM = L::NM;
-    constexpr int U = H >= 4 ? 2 : (H == 2 ? 4 : 8);  // tiles per batch
-    constexpr int MA = (8 * U + 31) / 32;             // a2b registers per lane
-
     extern __shared__ __align__(16) float smem[];
     float* part = smem;  // [2 * kNW] slots
     uint32_t* s_rwo = reinterpret_cast<uint32_t*>(smem + 2 * kNW * 8 * FS);
     Block<FS, kNW> blk;
     blk.init(a, s_rwo, part);
-    const int lane = blk.lane, g = blk.g, tq = blk.tq;
-    const uint32_t tb = blk.bound(blk.warp), te = blk.bound(blk.warp + 1);
-
-    bool fok[H];
-#pragma unroll
-    for (int h = 0; h < H; ++h) fok[h] = blk.f0 + 32 * h + 4 * g < a.K;
-
-    if (tb < te) {
-        uint32_t wl = blk.window_of(tb);
-        uint32_t next_bound = blk.s_rwo[wl + 1];
-        bool first_win = true;
-        float acc[NM][4];
-#pragma unroll
-        for (int m = 0; m < NM; ++m) acc[m][0] = acc[m][1] = acc[m][2] = acc[m][3] = 0.f;
-
-        uint32_t ma[MA];
-        uint64_t mb;
-        uint32_t mo;
-        auto load_meta = [&](uint32_t t) {
-#pragma unroll
-            for (int j = 0; j < MA; ++j) {
-                uint32_t e = 32 * j + lane;
-                uint32_t tile = t + e / 8;
-                ma[j] = (e < 8 * U && tile < te) ? __ldg(a.a2b + size_t(t) * 8 + e) : kPad;
-            }
-            uint32_t tl = t + uint32_t(lane);
-            bool ok = lane < U && tl < te;
-            mb = ok ? __ldg(reinterpret_cast<const unsigned long long*>(a.bits) + tl) : 0ull;
-            mo = ok ? __ldg(a.tc_offset + tl) : 0u;
-        };
-        load_meta(tb);
-
-        BitDecode dec;
-        dec.init(g, tq);
-        const float* Bl = a.B + blk.f0 + 4 * g;
-        for (uint32_t t = tb; t < te; t += U) {
-            float av0[U], av1[U];
-            float4 r0[U][H], r1[U][H];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const uint32_t i0 = __shfl_sync(0xffffffffu, ma[(8 * u) / 32], (8 * u + tq) & 31);
-                const uint32_t i1 = __shfl_sync(0xffffffffu, ma[(8 * u) / 32], (8 * u + tq + 4) & 31);
-                const uint64_t bm = shfl_u64(mb, u);
-                const uint32_t to = __shfl_sync(0xffffffffu, mo, u);
-                uint32_t x0, x1;
-                bool q0, q1;
-                dec.decode(bm, x0, x1, q0, q1);
-                av0[u] = q0 ? ldg_f32_ordered(a.vals + to + x0) : 0.f;
-                av1[u] = q1 ? ldg_f32_ordered(a.vals + to + x1) : 0.f;
-                const bool v0 = i0 < a.cols, v1 = i1 < a.cols;
-                const float* p0 = Bl + size_t(v0 ? i0 : 0) * a.K;
-                const float* p1 = Bl + size_t(v1 ? i1 : 0) * a.K;
-#pragma unroll
-                for (int h = 0; h < H; ++h) {
-                    r0[u][h] = (v0 && fok[h]) ? ldg_f4_ordered(p0 + 32 * h) : make_float4(0.f, 0.f, 0.f, 0.f);
-                    r1[u][h] = (v1 && fok[h]) ? ldg_f4_ordered(p1 + 32 * h) : make_float4(0.f, 0.f, 0.f, 0.f);
-                }
-            }
-            if (t + U < te) load_meta(t + U);
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const uint32_t tt = t + u;
-                if (tt >= te) break;
-                if (tt >= next_bound) {
-                    blk.flush(a, acc, wl, tb, te, first_win);
-                    first_win = false;
-#pragma unroll
-                    for (int m = 0; m < NM; ++m) acc[m][0] = acc[m][1] = acc[m][2] = acc[m][3] = 0.f;
-                    while (blk.s_rwo[wl + 1] <= tt) ++wl;
-                    next_bound = blk.s_rwo[wl + 1];
-                }
-                tile_mma<H, PREC>(acc, r0[u], r1[u], av0[u], av1[u]);
-            }
-        }
-        blk.flush(a, acc, wl, tb, te, first_win);
-    }
-    __syncthreads();
-    blk.finish(a);
+    direct_item<FS, PREC>(a, blk);
 }
 
 // Double-buffered register-direct kernel: the gathers of batch q + 1 are
@@ -381,6 +293,8 @@ int sm_count() {
     }
     return cached[dev];
 }
+
+uint32_t window_block_for(uint32_t w_cfg, uint32_t K) { return choose_config(w_cfg, K).wb; }
 
 int spmm_window_launch(const uint32_t* rwo, const uint32_t* tc_offset, const uint64_t* bits,
                        const uint32_t* a2b, const float* vals, uint32_t W, uint32_t w_cfg,

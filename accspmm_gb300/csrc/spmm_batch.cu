@@ -1,0 +1,277 @@
+// spmm_batch.cu -- many METCF matrices of different sizes and feature widths
+// in one persistent launch.
+//
+// A batch is a table of per-matrix descriptors in device memory.  Every
+// matrix is cut into the same work items (window block, feature slice) as a
+// one-matrix launch -- the window-block size comes from the same chooser -- so
+// each item's arithmetic, and therefore each result, is bit-identical to the
+// matrix's own accspmm_spmm_tf32 launch.  Items are numbered largest matrix
+// first; resident CTAs (two per SM) take items from an atomic counter until
+// none are left, so uneven matrices share the GPU without a tail of idle SMs.
+// A plan can be captured into a CUDA graph (counter reset + launch) and
+// replayed.
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "common.hpp"
+#include "device_util.cuh"
+#include "spmm_batch.hpp"
+#include "spmm_common.cuh"
+#include "spmm_direct.cuh"
+#include "spmm_internal.hpp"
+
+namespace accspmm {
+
+namespace {
+
+constexpr int kNW = kDirectNW;
+
+// Work items of one launch: descriptors sorted by item0 (first item).
+__device__ __forceinline__ uint32_t find_desc(const BatchDesc* __restrict__ d, uint32_t n,
+                                              uint32_t item) {
+    uint32_t lo = 0, hi = n;  // last desc with item0 <= item
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (d[mid].item0 <= item) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <int FS, int PREC>
+__global__ void __launch_bounds__(kNW * 32, 2)
+spmm_batch_kernel(const BatchDesc* __restrict__ desc, uint32_t n_desc, uint32_t total_items,
+                  uint32_t* __restrict__ counter) {
+    extern __shared__ __align__(16) float smem[];
+    float* part = smem;  // [2 kNW][8][FS]
+    uint32_t* s_rwo = reinterpret_cast<uint32_t*>(smem + 2 * kNW * 8 * FS);
+    __shared__ SpmmArgs s_args;
+    __shared__ uint32_t s_item, s_wbk, s_slice;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const uint32_t item = atomicAdd(counter, 1u);
+            s_item = item;
+            if (item < total_items) {
+                const uint32_t di = find_desc(desc, n_desc, item);
+                const BatchDesc& d = desc[di];
+                const uint32_t local = item - d.item0;
+                s_args = SpmmArgs{d.rwo, d.tc_offset, d.bits, d.a2b, d.vals, d.B, d.C, d.W, d.cols,
+                                  d.K, d.wb, d.n_slices, d.n_wblocks, 0};
+                s_wbk = local / d.n_slices;
+                s_slice = local - s_wbk * d.n_slices;
+            }
+        }
+        __syncthreads();
+        if (s_item >= total_items) break;
+        Block<FS, kNW> blk;
+        blk.init_item(s_args, s_wbk, s_slice, s_rwo, part);
+        direct_item_dispatch<FS, PREC>(s_args, blk);
+        __syncthreads();  // s_args, s_rwo and the slots are reused by the next item
+    }
+}
+
+template <int FS, int PREC>
+int launch_batch_t(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items,
+                   uint32_t max_wb, uint32_t* d_counter, cudaStream_t s) {
+    const size_t smem = size_t(2 * kNW * 8 * FS) * 4 + size_t(max_wb + 1) * 4;
+    static unsigned attr_set = 0;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 32 && !(attr_set & (1u << dev))) {
+        ACC_CUDA(cudaFuncSetAttribute(spmm_batch_kernel<FS, PREC>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+        attr_set |= 1u << dev;
+    }
+    if (smem > 100 * 1024) ACC_FAIL(ACCSPMM_ERROR_UNSUPPORTED, "window block too large for a batch");
+    const uint32_t grid = std::min<uint32_t>(total_items, uint32_t(sm_count()) * 2);
+    if (grid == 0) return ACCSPMM_SUCCESS;
+    spmm_batch_kernel<FS, PREC><<<grid, kNW * 32, smem, s>>>(d_desc, n_desc, total_items, d_counter);
+    ACC_LAUNCH_CHECK();
+    return ACCSPMM_SUCCESS;
+}
+
+}  // namespace
+
+int batch_fs_for(uint32_t max_k) { return max_k <= 32 ? 32 : max_k <= 64 ? 64 : 128; }
+
+int launch_batch(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items, uint32_t max_wb,
+                 uint32_t* d_counter, int fs, int precision, cudaStream_t s) {
+    ACC_CUDA(cudaMemsetAsync(d_counter, 0, 4, s));
+    const bool x3 = precision == ACCSPMM_PREC_3XTF32;
+    switch (fs) {
+        case 32: return x3 ? launch_batch_t<32, ACCSPMM_PREC_3XTF32>(d_desc, n_desc, total_items, max_wb, d_counter, s)
+                           : launch_batch_t<32, ACCSPMM_PREC_TF32>(d_desc, n_desc, total_items, max_wb, d_counter, s);
+        case 64: return x3 ? launch_batch_t<64, ACCSPMM_PREC_3XTF32>(d_desc, n_desc, total_items, max_wb, d_counter, s)
+                           : launch_batch_t<64, ACCSPMM_PREC_TF32>(d_desc, n_desc, total_items, max_wb, d_counter, s);
+        default: return x3 ? launch_batch_t<128, ACCSPMM_PREC_3XTF32>(d_desc, n_desc, total_items, max_wb, d_counter, s)
+                           : launch_batch_t<128, ACCSPMM_PREC_TF32>(d_desc, n_desc, total_items, max_wb, d_counter, s);
+    }
+}
+
+int make_batch_descs(const BatchInput* in, uint32_t n, int fs, std::vector<BatchDesc>* out,
+                     uint32_t* total_items, uint32_t* max_wb) {
+    std::vector<BatchDesc> d(n);
+    std::vector<uint64_t> work(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        const BatchInput& x = in[i];
+        if (x.K == 0 || x.K % 4) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "item %u: K=%u must be a positive multiple of 4", i, x.K);
+        if (!x.B || !x.C || ((reinterpret_cast<uintptr_t>(x.B) | reinterpret_cast<uintptr_t>(x.C)) & 15u))
+            ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "item %u: B and C must be 16-byte aligned device pointers", i);
+        const uint32_t wb = window_block_for(x.w_cfg, x.K);
+        const uint32_t slices = (x.K + uint32_t(fs) - 1) / uint32_t(fs);
+        d[i] = BatchDesc{x.rwo, x.tc_offset, x.bits, x.a2b, x.vals, x.B, x.C, x.W, x.cols, x.K,
+                         wb, slices, (x.W + wb - 1) / wb, 0, 0};
+        work[i] = uint64_t(x.T + x.W) * slices;
+    }
+    // largest matrix first
+    std::vector<uint32_t> order(n);
+    std::iota(order.begin(), order.end(), 0u);
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return work[a] > work[b]; });
+    out->clear();
+    uint64_t items = 0;
+    uint32_t mwb = 1;
+    for (uint32_t k = 0; k < n; ++k) {
+        BatchDesc x = d[order[k]];
+        if (x.W == 0) continue;
+        x.item0 = uint32_t(items);
+        x.index = order[k];
+        items += uint64_t(x.n_wblocks) * x.n_slices;
+        mwb = std::max(mwb, x.wb);
+        out->push_back(x);
+    }
+    if (items > 0x7FFFFFFFull) ACC_FAIL(ACCSPMM_ERROR_OVERFLOW, "too many work items in a batch");
+    *total_items = uint32_t(items);
+    *max_wb = mwb;
+    return ACCSPMM_SUCCESS;
+}
+
+}  // namespace accspmm
+
+// ---------------------------------------------------------------------------
+// C ABI: batch plans
+// ---------------------------------------------------------------------------
+using namespace accspmm;
+
+struct accspmm_batch {
+    int device = 0;
+    int precision = ACCSPMM_PREC_TF32;
+    int fs = 64;
+    uint32_t n_desc = 0, total_items = 0, max_wb = 1;
+    BatchDesc* d_desc = nullptr;
+    uint32_t* d_counter = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph = nullptr;
+};
+
+extern "C" {
+
+int accspmm_batch_create(const accspmm_batch_item_t* items, uint32_t n, int32_t precision,
+                         accspmm_batch_t** out) {
+    clear_error();
+    if (!out || (n && !items)) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "null argument");
+    if (precision != ACCSPMM_PREC_TF32 && precision != ACCSPMM_PREC_3XTF32)
+        ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "unknown precision %d", precision);
+    *out = nullptr;
+    std::vector<BatchInput> in(n);
+    uint32_t max_k = 4;
+    for (uint32_t i = 0; i < n; ++i) {
+        const accspmm_metcf_t* m = items[i].metcf;
+        if (!m || m->space != ACCSPMM_DEVICE) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "item %u: METCF must be on the device", i);
+        in[i] = BatchInput{m->row_window_offset, m->tc_offset, m->tc_local_bit, m->sparse_a2b, m->data,
+                           items[i].B, items[i].C, m->num_windows, m->num_windows, m->num_tiles,
+                           m->cols, items[i].K};
+        max_k = std::max(max_k, items[i].K);
+    }
+    auto* b = new accspmm_batch();
+    cudaGetDevice(&b->device);
+    b->precision = precision;
+    b->fs = batch_fs_for(max_k);
+    std::vector<BatchDesc> d;
+    int st = make_batch_descs(in.data(), n, b->fs, &d, &b->total_items, &b->max_wb);
+    if (st) {
+        delete b;
+        return st;
+    }
+    b->n_desc = uint32_t(d.size());
+    if (cudaMalloc(&b->d_desc, sizeof(BatchDesc) * std::max<size_t>(1, d.size())) != cudaSuccess ||
+        cudaMalloc(&b->d_counter, 4) != cudaSuccess) {
+        cudaFree(b->d_desc);
+        delete b;
+        ACC_FAIL(ACCSPMM_ERROR_ALLOC, "device allocation of the batch table failed");
+    }
+    if (!d.empty() && cudaMemcpy(b->d_desc, d.data(), sizeof(BatchDesc) * d.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(b->d_desc);
+        cudaFree(b->d_counter);
+        delete b;
+        ACC_FAIL(ACCSPMM_ERROR_CUDA, "copy of the batch table failed");
+    }
+    *out = b;
+    return ACCSPMM_SUCCESS;
+}
+
+int accspmm_batch_run(accspmm_batch_t* b, void* stream) {
+    clear_error();
+    if (!b) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "null batch");
+    if (b->total_items == 0) return ACCSPMM_SUCCESS;
+    return launch_batch(b->d_desc, b->n_desc, b->total_items, b->max_wb, b->d_counter, b->fs,
+                        b->precision, as_stream(stream));
+}
+
+int accspmm_batch_capture(accspmm_batch_t* b, void* stream) {
+    clear_error();
+    if (!b) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "null batch");
+    cudaStream_t s = as_stream(stream);
+    if (!s) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "graph capture needs a non-default stream");
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        cudaGraphDestroy(b->graph);
+        b->exec = nullptr;
+        b->graph = nullptr;
+    }
+    // make sure the kernels' attributes are set outside the capture
+    ACC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int st = accspmm_batch_run(b, stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (st) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) ACC_FAIL(ACCSPMM_ERROR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&b->exec, g, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        ACC_FAIL(ACCSPMM_ERROR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+    }
+    b->graph = g;
+    return ACCSPMM_SUCCESS;
+}
+
+int accspmm_batch_launch_graph(accspmm_batch_t* b, void* stream) {
+    clear_error();
+    if (!b || !b->exec) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "batch has no captured graph");
+    ACC_CUDA(cudaGraphLaunch(b->exec, as_stream(stream)));
+    return ACCSPMM_SUCCESS;
+}
+
+int accspmm_batch_info(const accspmm_batch_t* b, uint32_t* n_items, uint32_t* work_items,
+                       uint32_t* slice_width) {
+    clear_error();
+    if (!b) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "null batch");
+    if (n_items) *n_items = b->n_desc;
+    if (work_items) *work_items = b->total_items;
+    if (slice_width) *slice_width = uint32_t(b->fs);
+    return ACCSPMM_SUCCESS;
+}
+
+void accspmm_batch_destroy(accspmm_batch_t* b) {
+    if (!b) return;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    cudaFree(b->d_desc);
+    cudaFree(b->d_counter);
+    delete b;
+}
+
+}  // extern "C"

@@ -207,6 +207,7 @@ struct Block {
     float* part;
     int lane, warp, g, tq;
 
+    // work item of a CTA of a one-matrix launch
     __device__ __forceinline__ void init(const SpmmArgs& a, uint32_t* s_rwo_mem, float* part_mem) {
         uint32_t wbk, slice;
         if (a.slice_major) {
@@ -216,6 +217,12 @@ struct Block {
             wbk = blockIdx.x / a.n_slices;
             slice = blockIdx.x - wbk * a.n_slices;
         }
+        init_item(a, wbk, slice, s_rwo_mem, part_mem);
+    }
+
+    // explicit work item (window block wbk, feature slice `slice`)
+    __device__ __forceinline__ void init_item(const SpmmArgs& a, uint32_t wbk, uint32_t slice,
+                                              uint32_t* s_rwo_mem, float* part_mem) {
         w0 = wbk * a.wb;
         const uint32_t w1 = min(w0 + a.wb, a.W);
         nwin = w1 - w0;

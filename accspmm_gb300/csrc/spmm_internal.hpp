@@ -11,6 +11,9 @@ namespace accspmm {
 
 int sm_count();
 
+// Windows per CTA the launch-shape chooser picks for (w_cfg, K).
+uint32_t window_block_for(uint32_t w_cfg, uint32_t K);
+
 // One launch of the window-block kernel over W windows described by rwo;
 // the launch shape is chosen from (w_cfg, K).
 int spmm_window_launch(const uint32_t* rwo, const uint32_t* tc_offset, const uint64_t* bits,

@@ -50,6 +50,10 @@ def parse():
     p.add_argument("--no-sweep", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-host-build", action="store_true")
+    p.add_argument("--workload", default="scale", choices=["scale", "batch", "precision"],
+                   help="scale: the 1M-row SpMM (headline); batch: many graphs in one "
+                        "launch vs one launch each; precision: TF32 vs 3xTF32 vs FP64")
+    p.add_argument("--graphs", type=int, default=512)
     p.add_argument("--profile", type=int, default=0, metavar="LAUNCHES",
                    help="only build METCF on the GPU and run LAUNCHES plain SpMM launches "
                         "(no timing): the command profiled by ncu")
@@ -413,10 +417,107 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def batch_workload(n_graphs: int, seed: int, row_lo: int = 1000, row_hi: int = 20000):
+    """n power-law graphs with rows log-uniform in [row_lo, row_hi], mean
+    degree uniform in [4, 64], values uniform[0, 1), K from {64, 128}."""
+    from accspmm_gb300 import synth
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_graphs):
+        rows = int(np.exp(rng.uniform(np.log(row_lo), np.log(row_hi))))
+        mean = float(rng.uniform(4, 64))
+        k = int(rng.choice([64, 128]))
+        deg = synth.powerlaw_degrees(rows, 2.1, mean, min(rows, 4096), rng)
+        r = np.repeat(np.arange(rows, dtype=np.int64), deg)
+        c = rng.integers(0, rows, size=r.size)
+        r, c = synth._dedupe_sorted(r, c, rows)
+        v = rng.random(r.size, dtype=np.float32)
+        rp, ci, vals = synth.coo_to_csr(rows, r, c, v)
+        out.append((dict(rows=rows, cols=rows, nnz=len(ci), row_ptr=rp, col_idx=ci, data=vals), k))
+    return out
+
+
+def run_batch(args):
+    """Batched SpMM: one persistent launch (replayed as a CUDA graph) over all
+    graphs against one plain launch per graph, same inputs, same results."""
+    import torch
+
+    from accspmm_gb300 import api, capi
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    prec = capi.PREC_3XTF32 if args.precision == "3xtf32" else capi.PREC_TF32
+    graphs = batch_workload(args.graphs, args.seed)
+    gen = torch.Generator(device=dev).manual_seed(args.seed)
+    items, flops = [], 0.0
+    for csr, k in graphs:
+        m = api.DeviceMETCF.from_csr(api.DeviceCSR.upload(csr))
+        B = torch.rand((csr["cols"], k), device=dev, generator=gen) * 2 - 1
+        C = torch.empty((m.c_rows, k), device=dev)
+        items.append((m, B, C, k))
+        flops += 2.0 * csr["nnz"] * k
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    b = api.Batch(items, prec)
+    b.run(s)
+    s.synchronize()
+    b.capture(s)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        s.synchronize()
+        e0.record(s)
+        for _ in range(reps):
+            fn()
+        e1.record(s)
+        s.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def separate():
+        for m, B, C, k in items:
+            m.spmm(B, C, k, prec, s)
+
+    with ClockSampler(0) as clk:
+        t_graph = timed(lambda: b.launch_graph(s), args.steps)
+        t_batch = timed(lambda: b.run(s), args.steps)
+        t_sep = timed(separate, max(3, args.steps // 10))
+    # the batched results equal the separate launches bit for bit
+    ref = [C.clone() for _, _, C, _ in items]
+    b.launch_graph(s)
+    s.synchronize()
+    same = all(torch.equal(C, r) for (_, _, C, _), r in zip(items, ref))
+    n_items, work, fs = b.info()
+    nnz = sum(c["nnz"] for c, _ in graphs)
+    rows = sum(c["rows"] for c, _ in graphs)
+    out = {
+        "metric": METRIC, "value": round(flops / (t_graph * 1e-3) / 1e9, 2), "unit": UNIT,
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_graph, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": args.precision, "data": "synthetic",
+        "config": {"workload": f"{args.graphs} power-law graphs, rows log-uniform in [1000, 20000] "
+                               "(one tenth of the stated [1000, 200000] range), mean degree "
+                               "uniform in [4, 64], K in {64, 128}",
+                   "graphs": args.graphs, "rows": rows, "nnz": nnz, "work_items": work,
+                   "slice_width": fs},
+        "batch": {"graph_replay_ms": round(t_graph, 4), "one_launch_ms": round(t_batch, 4),
+                  "separate_launches_ms": round(t_sep, 4),
+                  "speedup_vs_separate": round(t_sep / t_graph, 2),
+                  "requests_per_s_graph": round(args.graphs / (t_graph * 1e-3), 1),
+                  "requests_per_s_separate": round(args.graphs / (t_sep * 1e-3), 1),
+                  "bitwise_equal_to_separate": bool(same)},
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_ours(args)
 

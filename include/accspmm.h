@@ -234,6 +234,36 @@ int accspmm_time_spmm(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp,
                       int32_t precision, int32_t warmup, int32_t exe,
                       float* avg_ms, void* stream);
 
+/* ---- batches ------------------------------------------------------------- */
+/* No counterpart in the reference (one matrix per process there).  A batch
+ * plan runs many device METCF matrices of different sizes and feature widths
+ * in one persistent launch: work items (window block x feature slice) of all
+ * matrices are numbered largest matrix first and taken by resident CTAs from
+ * an atomic counter.  Each item is computed exactly as in the matrix's own
+ * accspmm_spmm_tf32 launch, so results are bit-identical to one launch per
+ * matrix.  The plan keeps the pointers it was given: B and C contents may
+ * change between runs, the buffers may not move or be freed. */
+typedef struct accspmm_batch_item {
+    const accspmm_metcf_t* metcf;  /* device METCF */
+    const float* B;                /* cols x K */
+    float* C;                      /* 8 num_windows x K */
+    uint32_t K;
+} accspmm_batch_item_t;
+
+typedef struct accspmm_batch accspmm_batch_t;
+
+int accspmm_batch_create(const accspmm_batch_item_t* items, uint32_t n,
+                         int32_t precision, accspmm_batch_t** batch);
+/* One persistent launch on `stream` (counter reset + kernel). */
+int accspmm_batch_run(accspmm_batch_t* batch, void* stream);
+/* Captures accspmm_batch_run into a CUDA graph on `stream` (not the legacy
+ * default stream) and instantiates it; accspmm_batch_launch_graph replays it. */
+int accspmm_batch_capture(accspmm_batch_t* batch, void* stream);
+int accspmm_batch_launch_graph(accspmm_batch_t* batch, void* stream);
+int accspmm_batch_info(const accspmm_batch_t* batch, uint32_t* n_items,
+                       uint32_t* work_items, uint32_t* slice_width);
+void accspmm_batch_destroy(accspmm_batch_t* batch);
+
 /* Synchronises `stream`, then reports (and clears) the sticky status of the
  * SpMM kernels' bounded waits on the current device: ACCSPMM_ERROR_TIMEOUT if
  * a wait on an asynchronous copy expired since the last call (the affected
