@@ -248,6 +248,17 @@ class DeviceMETCF(DeviceObject):
         call("accspmm_spmm_tf32", self.ref, C.c_void_p(_addr(B)), C.c_void_p(_addr(C_out)), K,
              precision, _stream(stream))
 
+    def autotune(self, B, C_out, K: int, precision: int = capi.PREC_TF32, stream=None) -> dict:
+        """Times the candidate launch shapes and keeps the fastest for this
+        matrix's signature (overwrites C_out)."""
+        r = capi.TUNE()
+        call("accspmm_autotune_metcf", self.ref, C.c_void_p(_addr(B)), C.c_void_p(_addr(C_out)),
+             K, precision, _stream(stream), C.byref(r))
+        return dict(kernel={0: "direct", 4: "double-buffered"}.get(r.kernel, str(r.kernel)),
+                    slice_width=r.slice_width, windows_per_cta=r.windows_per_cta,
+                    best_ms=round(r.best_ms, 4), default_ms=round(r.default_ms, 4),
+                    candidates=r.candidates)
+
 
 class DeviceADPBME(DeviceObject):
     _destroy = "accspmm_adpbme_destroy"
@@ -305,6 +316,55 @@ class Batch:
     def destroy(self):
         if self.h:
             load().accspmm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching request server over resident device METCF graphs.
+
+    Host B / C buffers (torch pinned tensors or raw addresses) must stay
+    valid until wait() returns for their request."""
+
+    def __init__(self, graphs, hbm_budget_bytes, max_batch=64, streams=4):
+        arr = (METCF * len(graphs))()
+        for i, g in enumerate(graphs):
+            arr[i] = g.struct
+        self._keep = list(graphs)
+        cfg = capi.SERVERCFG(hbm_budget_bytes, max_batch, streams)
+        h = C.c_void_p()
+        call("accspmm_server_create", arr, len(graphs), C.byref(cfg), C.byref(h))
+        self.h = h
+
+    def submit(self, graph: int, B_host, C_host, K: int, precision=capi.PREC_TF32, chain=1) -> int:
+        rid = C.c_uint64()
+        call("accspmm_server_submit", self.h, graph, C.c_void_p(_addr(B_host)),
+             C.c_void_p(_addr(C_host)), K, precision, chain, C.byref(rid))
+        return rid.value
+
+    def wait(self, rid: int, timeout_ms: int = -1) -> int:
+        """Returns the request's status (0 on success)."""
+        return load().accspmm_server_wait(self.h, rid, timeout_ms)
+
+    def cancel(self, rid: int) -> int:
+        return load().accspmm_server_cancel(self.h, rid)
+
+    def stats(self) -> dict:
+        st = capi.SERVERSTATS()
+        call("accspmm_server_stats", self.h, C.byref(st))
+        return {k: getattr(st, k) for k, _ in capi.SERVERSTATS._fields_}
+
+    def reset_stats(self):
+        call("accspmm_server_reset_stats", self.h)
+
+    def destroy(self):
+        if self.h:
+            load().accspmm_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

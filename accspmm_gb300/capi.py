@@ -65,6 +65,23 @@ class ADPBME(C.Structure):
                 ("data", f32p), ("space", i32), ("owned", i32)]
 
 
+class TUNE(C.Structure):
+    _fields_ = [("kernel", i32), ("slice_width", u32), ("windows_per_cta", u32),
+                ("best_ms", C.c_float), ("default_ms", C.c_float), ("candidates", u32)]
+
+
+class SERVERCFG(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_batch", u32), ("streams", u32)]
+
+
+class SERVERSTATS(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("rejected", C.c_uint64),
+                ("cancelled", C.c_uint64), ("launches", C.c_uint64), ("p50_ms", C.c_double),
+                ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("max_ms", C.c_double),
+                ("throughput_rps", C.c_double), ("mean_batch", C.c_double),
+                ("peak_bytes", C.c_size_t)]
+
+
 class BATCHITEM(C.Structure):
     _fields_ = [("metcf", C.POINTER(METCF)), ("B", vp), ("C", vp), ("K", u32)]
 
@@ -90,6 +107,15 @@ _SIGS = {
     "accspmm_spmm_tf32": ([C.POINTER(METCF), vp, vp, u32, i32, vp], C.c_int),
     "accspmm_spmm_adaptive": ([C.POINTER(ADPBME), vp, vp, u32, u32, i32, vp], C.c_int),
     "accspmm_device_status": ([vp], C.c_int),
+    "accspmm_autotune_metcf": ([C.POINTER(METCF), vp, vp, u32, i32, vp, C.POINTER(TUNE)], C.c_int),
+    "accspmm_autotune_clear": ([], None),
+    "accspmm_server_create": ([C.POINTER(METCF), u32, C.POINTER(SERVERCFG), C.POINTER(vp)], C.c_int),
+    "accspmm_server_submit": ([vp, u32, vp, vp, u32, i32, u32, C.POINTER(C.c_uint64)], C.c_int),
+    "accspmm_server_wait": ([vp, C.c_uint64, i32], C.c_int),
+    "accspmm_server_cancel": ([vp, C.c_uint64], C.c_int),
+    "accspmm_server_stats": ([vp, C.POINTER(SERVERSTATS)], C.c_int),
+    "accspmm_server_reset_stats": ([vp], C.c_int),
+    "accspmm_server_destroy": ([vp], None),
     "accspmm_batch_create": ([C.POINTER(BATCHITEM), u32, i32, C.POINTER(vp)], C.c_int),
     "accspmm_batch_run": ([vp, vp], C.c_int),
     "accspmm_batch_capture": ([vp, vp], C.c_int),

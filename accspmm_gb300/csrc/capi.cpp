@@ -324,6 +324,14 @@ int accspmm_spmm_adaptive_noalloc(const accspmm_adpbme_t* adp, const float* B, f
 
 uint32_t accspmm_noalloc_max_c_rows(void) { return noalloc_max_c_rows(); }
 
+int accspmm_autotune_metcf(const accspmm_metcf_t* metcf, const float* B, float* C, uint32_t K,
+                           int32_t precision, void* stream, accspmm_tune_result_t* result) {
+    clear_error();
+    return autotune_impl(metcf, B, C, K, precision, stream, result);
+}
+
+void accspmm_autotune_clear(void) { autotune_clear(); }
+
 int accspmm_device_status(void* stream) {
     clear_error();
     return device_status_impl(stream);

@@ -24,7 +24,10 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
+#include <vector>
 
 #include "common.hpp"
 #include "device_util.cuh"
@@ -227,35 +230,62 @@ int env_int(const char* name, int dflt) {
     return e && *e ? std::atoi(e) : dflt;
 }
 
-// Launch shape from (W, K).  Measured on GB300 with the 1M-row power-law
-// workload: 128-column slices (the whole row of B for K <= 128) and 16
-// windows per CTA are fastest for K >= 128; narrower K uses a slice of K.
-// Every field can be overridden through the environment for tuning
-// (ACCSPMM_KERNEL, _FS, _WB, _NW, _ORDER, _HINTS).
-Config choose_config(uint32_t W, uint32_t K) {
+int env_int(const char* name, int dflt);
+
+// Tuned launch shapes, by matrix signature (autotune below).
+struct TuneKey {
+    uint32_t w, t, k;
+    int prec;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(w, t, k, prec) < std::tie(o.w, o.t, o.k, o.prec);
+    }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, Config> g_tuned;
+// configuration forced by the autotuner while it times a candidate
+thread_local const Config* g_forced = nullptr;
+
+// Launch shape from (W, T, K, precision).  Defaults measured on GB300 with
+// the 1M-row power-law workload: 128-column slices (the whole row of B for
+// K <= 128) and 16 windows per CTA are fastest for K >= 128; narrower K uses
+// a slice of K.  A shape found by accspmm_autotune_metcf for the same
+// signature replaces the default; environment variables override both for
+// experiments (ACCSPMM_KERNEL, _FS, _WB, _NW, _ORDER, _HINTS).
+Config choose_config(uint32_t W, uint32_t T, uint32_t K, int precision) {
+    if (g_forced) return *g_forced;
     Config c;
     c.kernel = kDirect;
+    c.fs = K <= 32 ? 32 : K <= 64 ? 64 : 128;
+    c.nw = c.fs == 32 ? 8 : 4;
+    c.hints = 1;
+    c.slice_major = 0;
+    {
+        uint64_t slices = (K + c.fs - 1) / c.fs;
+        // 16 windows per CTA, fewer for small matrices so that every SM gets work
+        uint64_t want = uint64_t(sm_count()) * 4;
+        uint64_t wb = std::max<uint64_t>(1, (uint64_t(W) * slices) / want);
+        c.wb = uint32_t(std::min<uint64_t>(16, std::max<uint64_t>(2, wb)));
+    }
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tuned.find(TuneKey{W, T, K, precision});
+        if (it != g_tuned.end()) c = it->second;
+    }
     if (const char* e = std::getenv("ACCSPMM_KERNEL"))
         c.kernel = std::strcmp(e, "pipe") == 0   ? kPipe
                    : std::strcmp(e, "bulk") == 0 ? kBulk
                    : std::strcmp(e, "lean") == 0 ? kLean
                    : std::strcmp(e, "db") == 0   ? kDb
                                                  : kDirect;
-    c.fs = K <= 32 ? 32 : K <= 64 ? 64 : 128;
     int fs = env_int("ACCSPMM_FS", 0);
     if (fs == 32 || fs == 64 || fs == 128) c.fs = fs;
-    c.nw = env_int("ACCSPMM_NW", c.fs == 32 ? 8 : 4) == 4 ? 4 : 8;
+    int nw = env_int("ACCSPMM_NW", 0);
+    if (nw == 2 || nw == 4 || nw == 8) c.nw = nw;
     if (c.kernel == kPipe && c.fs >= 64) c.nw = 4;  // stage ring must fit in shared memory
-    if (c.kernel == kBulk) c.nw = env_int("ACCSPMM_NW", 4) == 2 ? 2 : 4;
-    c.hints = env_int("ACCSPMM_HINTS", 1) ? 1 : 0;
-    uint32_t slices = (K + c.fs - 1) / c.fs;
-    // 16 windows per CTA, fewer for small matrices so that every SM gets work
-    uint64_t want = uint64_t(sm_count()) * 4;
-    uint64_t wb = std::max<uint64_t>(1, (uint64_t(W) * slices) / want);
-    c.wb = uint32_t(std::min<uint64_t>(16, std::max<uint64_t>(2, wb)));
+    if (c.kernel == kBulk && c.nw == 8) c.nw = 4;
+    c.hints = env_int("ACCSPMM_HINTS", c.hints) ? 1 : 0;
     int wbe = env_int("ACCSPMM_WB", 0);
     if (wbe >= 1 && wbe <= 1024) c.wb = uint32_t(wbe);
-    c.slice_major = 0;
     if (const char* e = std::getenv("ACCSPMM_ORDER")) c.slice_major = std::strcmp(e, "slice") == 0;
     return c;
 }
@@ -294,16 +324,19 @@ int sm_count() {
     return cached[dev];
 }
 
-uint32_t window_block_for(uint32_t w_cfg, uint32_t K) { return choose_config(w_cfg, K).wb; }
+uint32_t window_block_for(uint32_t w_cfg, uint32_t T, uint32_t K, int precision) {
+    return choose_config(w_cfg, T, K, precision).wb;
+}
 
 int spmm_window_launch(const uint32_t* rwo, const uint32_t* tc_offset, const uint64_t* bits,
                        const uint32_t* a2b, const float* vals, uint32_t W, uint32_t w_cfg,
-                       uint32_t cols, const float* B, float* C, uint32_t K, int precision,
-                       cudaStream_t s) {
+                       uint32_t T, uint32_t cols, const float* B, float* C, uint32_t K,
+                       int precision, cudaStream_t s) {
     if (W == 0) return ACCSPMM_SUCCESS;
-    // the launch shape depends only on (w_cfg, K), so both entry points cut a
-    // matrix into the same pieces and sum partial windows in the same order
-    Config cfg = choose_config(w_cfg, K);
+    // the launch shape depends only on (w_cfg, T, K, precision), so every
+    // entry point cuts a matrix into the same pieces and sums partial windows
+    // in the same order
+    Config cfg = choose_config(w_cfg, T, K, precision);
     SpmmArgs a{rwo, tc_offset, bits, a2b, vals, B, C, W, cols, K, cfg.wb,
                (K + uint32_t(cfg.fs) - 1) / uint32_t(cfg.fs), (W + cfg.wb - 1) / cfg.wb,
                cfg.slice_major};
@@ -345,8 +378,8 @@ int spmm_tf32_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t 
     int st = check_dense(B, C, K, precision);
     if (st) return st;
     return spmm_window_launch(m->row_window_offset, m->tc_offset, m->tc_local_bit, m->sparse_a2b,
-                              m->data, m->num_windows, m->num_windows, m->cols, B, C, K, precision,
-                              as_stream(stream));
+                              m->data, m->num_windows, m->num_windows, m->num_tiles, m->cols, B, C,
+                              K, precision, as_stream(stream));
 }
 
 int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uint32_t c_rows,
@@ -366,7 +399,7 @@ int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uin
     rwo_from_row_indices_kernel<<<(Weff + 1 + 255) / 256, 256, 0, s>>>(ad->row_indices, T, Weff, rwo, err);
     ACC_LAUNCH_CHECK();
     return spmm_window_launch(rwo, ad->tc_offset, ad->tc_local_bit, ad->sparse_a2b, ad->data, Weff,
-                              (ad->rows + kWin - 1) / kWin, ad->cols, B, C, K, precision, s);
+                              (ad->rows + kWin - 1) / kWin, T, ad->cols, B, C, K, precision, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -427,7 +460,89 @@ int spmm_adaptive_noalloc_impl(const accspmm_adpbme_t* ad, const float* B, float
     rwo_from_row_indices_kernel<<<(Weff + 1 + 255) / 256, 256, 0, s>>>(ad->row_indices, T, Weff, rwo, err);
     ACC_LAUNCH_CHECK();
     return spmm_window_launch(rwo, ad->tc_offset, ad->tc_local_bit, ad->sparse_a2b, ad->data, Weff,
-                              (ad->rows + kWin - 1) / kWin, ad->cols, B, C, K, precision, s);
+                              (ad->rows + kWin - 1) / kWin, T, ad->cols, B, C, K, precision, s);
+}
+
+// Times the candidate launch shapes on (m, B, C) and keeps the fastest for
+// m's signature.  C is overwritten.
+int autotune_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K, int precision,
+                  void* stream, accspmm_tune_result_t* out) {
+    if (!m || m->space != ACCSPMM_DEVICE) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "METCF must be on the device");
+    int st = check_dense(B, C, K, precision);
+    if (st) return st;
+    cudaStream_t s = as_stream(stream);
+    const TuneKey key{m->num_windows, m->num_tiles, K, precision};
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tuned.erase(key);
+    }
+    const Config dflt = choose_config(m->num_windows, m->num_tiles, K, precision);
+    std::vector<Config> cand;
+    for (int kernel : {int(kDirect), int(kDb)})
+        for (int fs : {32, 64, 128}) {
+            if (fs > 32 && uint32_t(fs / 2) >= K) continue;  // slices far wider than K
+            for (uint32_t wb : {4u, 8u, 16u, 32u}) {
+                Config c = dflt;
+                c.kernel = kernel;
+                c.fs = fs;
+                c.wb = wb;
+                c.slice_major = 0;
+                cand.push_back(c);
+            }
+        }
+    cudaEvent_t e0, e1;
+    ACC_CUDA(cudaEventCreate(&e0));
+    ACC_CUDA(cudaEventCreate(&e1));
+    auto time_cfg = [&](const Config& c, float* ms) -> int {
+        g_forced = &c;
+        int r = 0;
+        for (int i = 0; i < 1 && !r; ++i) r = spmm_tf32_impl(m, B, C, K, precision, stream);
+        cudaEventRecord(e0, s);
+        for (int i = 0; i < 3 && !r; ++i) r = spmm_tf32_impl(m, B, C, K, precision, stream);
+        cudaEventRecord(e1, s);
+        g_forced = nullptr;
+        if (r) return r;
+        ACC_CUDA(cudaEventSynchronize(e1));
+        ACC_CUDA(cudaEventElapsedTime(ms, e0, e1));
+        *ms /= 3.f;
+        return ACCSPMM_SUCCESS;
+    };
+    float best_ms = 1e30f, dflt_ms = 0.f;
+    Config best = dflt;
+    st = time_cfg(dflt, &dflt_ms);
+    if (!st) {
+        best_ms = dflt_ms;
+        for (const Config& c : cand) {
+            float ms = 0.f;
+            st = time_cfg(c, &ms);
+            if (st) break;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = c;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) return st;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tuned[key] = best;
+    }
+    if (out) {
+        out->kernel = best.kernel;
+        out->slice_width = uint32_t(best.fs);
+        out->windows_per_cta = best.wb;
+        out->best_ms = best_ms;
+        out->default_ms = dflt_ms;
+        out->candidates = uint32_t(cand.size()) + 1;
+    }
+    return ACCSPMM_SUCCESS;
+}
+
+void autotune_clear() {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tuned.clear();
 }
 
 int device_status_impl(void* stream) { return bulk_status(as_stream(stream), true); }

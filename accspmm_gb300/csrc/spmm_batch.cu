@@ -109,8 +109,8 @@ int launch_batch(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items,
     }
 }
 
-int make_batch_descs(const BatchInput* in, uint32_t n, int fs, std::vector<BatchDesc>* out,
-                     uint32_t* total_items, uint32_t* max_wb) {
+int make_batch_descs(const BatchInput* in, uint32_t n, int fs, int precision,
+                     std::vector<BatchDesc>* out, uint32_t* total_items, uint32_t* max_wb) {
     std::vector<BatchDesc> d(n);
     std::vector<uint64_t> work(n);
     for (uint32_t i = 0; i < n; ++i) {
@@ -118,7 +118,7 @@ int make_batch_descs(const BatchInput* in, uint32_t n, int fs, std::vector<Batch
         if (x.K == 0 || x.K % 4) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "item %u: K=%u must be a positive multiple of 4", i, x.K);
         if (!x.B || !x.C || ((reinterpret_cast<uintptr_t>(x.B) | reinterpret_cast<uintptr_t>(x.C)) & 15u))
             ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "item %u: B and C must be 16-byte aligned device pointers", i);
-        const uint32_t wb = window_block_for(x.w_cfg, x.K);
+        const uint32_t wb = window_block_for(x.w_cfg, x.T, x.K, precision);
         const uint32_t slices = (x.K + uint32_t(fs) - 1) / uint32_t(fs);
         d[i] = BatchDesc{x.rwo, x.tc_offset, x.bits, x.a2b, x.vals, x.B, x.C, x.W, x.cols, x.K,
                          wb, slices, (x.W + wb - 1) / wb, 0, 0};
@@ -188,7 +188,7 @@ int accspmm_batch_create(const accspmm_batch_item_t* items, uint32_t n, int32_t 
     b->precision = precision;
     b->fs = batch_fs_for(max_k);
     std::vector<BatchDesc> d;
-    int st = make_batch_descs(in.data(), n, b->fs, &d, &b->total_items, &b->max_wb);
+    int st = make_batch_descs(in.data(), n, b->fs, precision, &d, &b->total_items, &b->max_wb);
     if (st) {
         delete b;
         return st;

@@ -46,8 +46,8 @@ struct BatchInput {
 int batch_fs_for(uint32_t max_k);
 
 // Descriptors in launch order (largest first), with item numbering.
-int make_batch_descs(const BatchInput* in, uint32_t n, int fs, std::vector<BatchDesc>* out,
-                     uint32_t* total_items, uint32_t* max_wb);
+int make_batch_descs(const BatchInput* in, uint32_t n, int fs, int precision,
+                     std::vector<BatchDesc>* out, uint32_t* total_items, uint32_t* max_wb);
 
 // Resets the work counter and launches the persistent batched kernel.
 int launch_batch(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items, uint32_t max_wb,

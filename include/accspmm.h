@@ -234,6 +234,32 @@ int accspmm_time_spmm(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp,
                       int32_t precision, int32_t warmup, int32_t exe,
                       float* avg_ms, void* stream);
 
+/* ---- autotuning ----------------------------------------------------------- */
+/* No counterpart in the reference (its launch shape is fixed: warps = K/32 or
+ * K/64 per CTA, one CTA per window or group).  Times the candidate launch
+ * shapes -- kernel variant (register-direct, double-buffered), feature-slice
+ * width (32/64/128 columns) and windows per CTA (4/8/16/32, the load-balance
+ * granularity) -- on this matrix with this B, and keeps the fastest for the
+ * matrix's signature (windows, tiles, K, precision) for the rest of the
+ * process: later plain, adaptive and batched calls on a matrix with that
+ * signature use it.  C is overwritten.  Results of different shapes agree
+ * within the TF32 tolerance but not bit for bit (partial windows are summed
+ * at different boundaries). */
+typedef struct accspmm_tune_result {
+    int32_t kernel;            /* 0 register-direct, 4 double-buffered */
+    uint32_t slice_width;      /* feature columns per CTA */
+    uint32_t windows_per_cta;
+    float best_ms;             /* time of the chosen shape */
+    float default_ms;          /* time of the default shape */
+    uint32_t candidates;
+} accspmm_tune_result_t;
+
+int accspmm_autotune_metcf(const accspmm_metcf_t* metcf, const float* B, float* C,
+                           uint32_t K, int32_t precision, void* stream,
+                           accspmm_tune_result_t* result);
+/* Forgets every tuned shape. */
+void accspmm_autotune_clear(void);
+
 /* ---- batches ------------------------------------------------------------- */
 /* No counterpart in the reference (one matrix per process there).  A batch
  * plan runs many device METCF matrices of different sizes and feature widths
@@ -263,6 +289,55 @@ int accspmm_batch_launch_graph(accspmm_batch_t* batch, void* stream);
 int accspmm_batch_info(const accspmm_batch_t* batch, uint32_t* n_items,
                        uint32_t* work_items, uint32_t* slice_width);
 void accspmm_batch_destroy(accspmm_batch_t* batch);
+
+/* ---- serving ------------------------------------------------------------- */
+/* No counterpart in the reference.  A continuous-batching request server over
+ * resident device METCF matrices.  Any thread submits requests (matrix index,
+ * host B of cols x K floats, host C of 8 num_windows x K floats, precision,
+ * chain 1 for C = A B or 2 for C = A (A B) on a square matrix); a worker
+ * thread admits pending requests in arrival order while their device memory
+ * (B, C, chain temporary) fits in hbm_budget_bytes and one of `streams`
+ * launch slots is free, runs up to max_batch of them in one batched launch
+ * (copies in, kernel, copies out on the slot's stream) and marks them done
+ * from a stream callback.  Batches on different slots overlap on the device.
+ * A request's result is the same bits alone or in any mix.  Host buffers
+ * should be pinned (cudaHostAlloc) for the copies to overlap; they must stay
+ * valid until accspmm_server_wait returns. */
+typedef struct accspmm_server accspmm_server_t;
+
+typedef struct accspmm_server_config {
+    size_t hbm_budget_bytes;  /* device memory for request buffers */
+    uint32_t max_batch;       /* requests per launch (0: 64) */
+    uint32_t streams;         /* launch slots in flight (0: 4) */
+} accspmm_server_config_t;
+
+typedef struct accspmm_server_stats {
+    uint64_t submitted, completed, rejected, cancelled, launches;
+    double p50_ms, p99_ms, mean_ms, max_ms;  /* submit -> completion */
+    double throughput_rps;                   /* completed / (last completion - first submit) */
+    double mean_batch;                       /* requests per launch */
+    size_t peak_bytes;                       /* peak admitted device memory */
+} accspmm_server_stats_t;
+
+/* The graphs must stay resident and unchanged for the server's lifetime. */
+int accspmm_server_create(const accspmm_metcf_t* graphs, uint32_t n_graphs,
+                          const accspmm_server_config_t* config,
+                          accspmm_server_t** server);
+/* Returns ACCSPMM_ERROR_ADMISSION if one request alone exceeds the budget. */
+int accspmm_server_submit(accspmm_server_t* server, uint32_t graph,
+                          const float* B_host, float* C_host, uint32_t K,
+                          int32_t precision, uint32_t chain,
+                          uint64_t* request_id);
+/* Blocks until the request is done (timeout_ms < 0: no limit); returns its
+ * status, ACCSPMM_ERROR_TIMEOUT if the limit passed first. */
+int accspmm_server_wait(accspmm_server_t* server, uint64_t request_id,
+                        int32_t timeout_ms);
+/* Cancels a request that has not been admitted yet. */
+int accspmm_server_cancel(accspmm_server_t* server, uint64_t request_id);
+int accspmm_server_stats(accspmm_server_t* server, accspmm_server_stats_t* stats);
+int accspmm_server_reset_stats(accspmm_server_t* server);
+/* Finishes the admitted and pending requests, then stops the worker. */
+void accspmm_server_destroy(accspmm_server_t* server);
 
 /* Synchronises `stream`, then reports (and clears) the sticky status of the
  * SpMM kernels' bounded waits on the current device: ACCSPMM_ERROR_TIMEOUT if

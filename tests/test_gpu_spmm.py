@@ -280,3 +280,32 @@ def test_tf32_rounding_is_rna_bit_exact():
     got = spmm_plain(m, B, K)[:n]
     want = np.vectorize(oracle.tf32_rna, otypes=[np.float32])(B)
     np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_autotune_picks_a_shape_that_is_used_and_correct():
+    g = gold("plsym1000")
+    csr = csr_of_gold(g)
+    m = device_metcf(csr)
+    h = m.to_numpy()
+    K = 64
+    B = np.random.default_rng(8).uniform(-1, 1, (csr["cols"], K)).astype(np.float32)
+    dB = torch_dev(B)
+    dC = empty_dev(m.c_rows, K)
+    try:
+        r = m.autotune(dB, dC, K)
+        # the default shape is one of the candidates and may win
+        assert r["slice_width"] in (32, 64, 128) and r["windows_per_cta"] >= 1
+        assert r["candidates"] > 1 and r["best_ms"] <= r["default_ms"] + 1e-6
+        got = spmm_plain(m, B, K)
+        c64 = oracle.spmm_metcf_f64(h, csr["cols"], B)
+        assert rel_fro(got, c64) < TOL_TF32_VS_F64
+        # the adaptive entry point uses the same tuned shape: identical rows
+        a = m.adpbme()
+        cr = a.c_rows()
+        dCa = empty_dev(cr, K)
+        a.spmm(dB, dCa, cr, K)
+        torch.cuda.synchronize()
+        n = min(cr, got.shape[0])
+        np.testing.assert_array_equal(dCa.cpu().numpy()[:n], got[:n])
+    finally:
+        capi.load().accspmm_autotune_clear()
