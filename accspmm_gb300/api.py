@@ -175,6 +175,8 @@ class DeviceObject:
 
     def destroy(self):
         if self.struct is not None and self.struct.owned:
+            if self.struct.space == capi.DEVICE:
+                _sync_device()  # queued work may still read the arrays
             getattr(load(), self._destroy)(C.byref(self.struct))
         self.struct = None
 
@@ -382,6 +384,15 @@ def time_spmm(metcf: DeviceMETCF | None, adp: DeviceADPBME | None, B, C_out, c_r
          C.c_void_p(_addr(B)), C.c_void_p(_addr(C_out)), c_rows, K, precision, warmup, exe,
          C.byref(ms), _stream(stream))
     return ms.value
+
+
+def _sync_device():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+    except ImportError:
+        pass
 
 
 def _sync(stream):

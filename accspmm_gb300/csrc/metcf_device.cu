@@ -356,6 +356,9 @@ int metcf_from_csr_device(const accspmm_csr_t* csr, accspmm_metcf_t* out, void* 
             csr->data, data.p);
         ACC_LAUNCH_CHECK();
     }
+    // the input CSR is read until here: finish before returning so that the
+    // caller may free it as soon as the call returns
+    ACC_CUDA(cudaStreamSynchronize(s));
     out->rows = rows;
     out->cols = cols;
     out->nnz = nnz;
@@ -438,6 +441,7 @@ int adpbme_from_metcf_device(const accspmm_metcf_t* m, uint32_t t_load, uint32_t
     }
     if (m->nnz)
         ACC_CUDA(cudaMemcpyAsync(data.p, m->data, size_t(m->nnz) * 4, cudaMemcpyDeviceToDevice, s));
+    ACC_CUDA(cudaStreamSynchronize(s));  // the input METCF may be freed after return
     a->rows = m->rows;
     a->cols = m->cols;
     a->nnz = m->nnz;

@@ -19,7 +19,11 @@
  *    products with the feature width are computed in 64-bit.
  *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default
  *    stream).  Device work is enqueued on it; functions that must return a
- *    host value (sizes, flags) synchronise that stream.
+ *    host value (sizes, flags) synchronise that stream, and the builders
+ *    (CSR, METCF, AdpBME) return only when their inputs are no longer read.
+ *    Inputs of the SpMM calls must stay allocated until the stream's work is
+ *    done; *_destroy frees immediately (cudaFree) and must not race with
+ *    queued work that reads the object.
  *  - Objects whose `space` is ACCSPMM_DEVICE hold device pointers.  Objects
  *    filled by the library own their arrays; release them with the matching
  *    *_destroy call.  Objects a caller fills by hand are never freed by the
