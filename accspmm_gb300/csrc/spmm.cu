@@ -46,14 +46,15 @@ __device__ __align__(16) float g_zero_row_direct[128] = {0.f};
 
 
 // One-matrix launch of the register-direct kernel: one CTA per work item.
-template <int FS, int PREC>
-__global__ void __launch_bounds__(kNW * 32, 2) spmm_window_kernel(const SpmmArgs a) {
+// U tiles per batch; MINB resident CTAs per SM (the register budget).
+template <int FS, int PREC, int U, int MINB>
+__global__ void __launch_bounds__(kNW * 32, MINB) spmm_window_kernel(const SpmmArgs a) {
     extern __shared__ __align__(16) float smem[];
     float* part = smem;  // [2 * kNW] slots
     uint32_t* s_rwo = reinterpret_cast<uint32_t*>(smem + 2 * kNW * 8 * FS);
     Block<FS, kNW> blk;
     blk.init(a, s_rwo, part);
-    direct_item<FS, PREC>(a, blk);
+    direct_item<FS, PREC, U>(a, blk);
 }
 
 // Double-buffered register-direct kernel: the gathers of batch q + 1 are
@@ -219,6 +220,7 @@ enum KernelKind { kDirect = 0, kPipe = 1, kBulk = 2, kLean = 3, kDb = 4 };
 struct Config {
     int kernel;
     int fs;
+    int occ;  // register-direct kernel: resident CTAs per SM (2 or 3)
     int nw;
     int hints;
     uint32_t wb;
@@ -246,25 +248,27 @@ std::map<TuneKey, Config> g_tuned;
 thread_local const Config* g_forced = nullptr;
 
 // Launch shape from (W, T, K, precision).  Defaults measured on GB300 with
-// the 1M-row power-law workload: 128-column slices (the whole row of B for
-// K <= 128) and 16 windows per CTA are fastest for K >= 128; narrower K uses
-// a slice of K.  A shape found by accspmm_autotune_metcf for the same
-// signature replaces the default; environment variables override both for
-// experiments (ACCSPMM_KERNEL, _FS, _WB, _NW, _ORDER, _HINTS).
+// the 1M-row power-law workload (K = 32 ... 256): the register-direct kernel
+// at 3 CTAs per SM (24 warps, a smaller gather batch per warp) with 64-column
+// slices (32 for K <= 32) and 32 windows per CTA, fewer for small matrices so
+// that every SM gets work; 10-20 % faster than 2 CTAs per SM with 128-column
+// slices.  A shape found by accspmm_autotune_metcf for the same signature
+// replaces the default; environment variables override both for experiments
+// (ACCSPMM_KERNEL, _FS, _OCC, _WB, _NW, _ORDER, _HINTS).
 Config choose_config(uint32_t W, uint32_t T, uint32_t K, int precision) {
     if (g_forced) return *g_forced;
     Config c;
     c.kernel = kDirect;
-    c.fs = K <= 32 ? 32 : K <= 64 ? 64 : 128;
+    c.fs = K <= 32 ? 32 : 64;
+    c.occ = 3;
     c.nw = c.fs == 32 ? 8 : 4;
     c.hints = 1;
     c.slice_major = 0;
     {
         uint64_t slices = (K + c.fs - 1) / c.fs;
-        // 16 windows per CTA, fewer for small matrices so that every SM gets work
         uint64_t want = uint64_t(sm_count()) * 4;
         uint64_t wb = std::max<uint64_t>(1, (uint64_t(W) * slices) / want);
-        c.wb = uint32_t(std::min<uint64_t>(16, std::max<uint64_t>(2, wb)));
+        c.wb = uint32_t(std::min<uint64_t>(32, std::max<uint64_t>(2, wb)));
     }
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
@@ -279,6 +283,8 @@ Config choose_config(uint32_t W, uint32_t T, uint32_t K, int precision) {
                                                  : kDirect;
     int fs = env_int("ACCSPMM_FS", 0);
     if (fs == 32 || fs == 64 || fs == 128) c.fs = fs;
+    int occ = env_int("ACCSPMM_OCC", 0);
+    if (occ == 2 || occ == 3) c.occ = occ;
     int nw = env_int("ACCSPMM_NW", 0);
     if (nw == 2 || nw == 4 || nw == 8) c.nw = nw;
     if (c.kernel == kPipe && c.fs >= 64) c.nw = 4;  // stage ring must fit in shared memory
@@ -290,23 +296,32 @@ Config choose_config(uint32_t W, uint32_t T, uint32_t K, int precision) {
     return c;
 }
 
-template <int FS, int PREC>
-int launch_direct(const SpmmArgs& a, cudaStream_t s) {
+template <int FS, int PREC, int U, int MINB>
+int launch_direct_t(const SpmmArgs& a, cudaStream_t s) {
     const size_t smem = size_t(2 * kNW * 8 * FS) * 4 + size_t(a.wb + 1) * 4;
     static unsigned attr_set = 0;  // one bit per device
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 32 && !(attr_set & (1u << dev))) {
-        ACC_CUDA(cudaFuncSetAttribute(spmm_window_kernel<FS, PREC>,
+        ACC_CUDA(cudaFuncSetAttribute(spmm_window_kernel<FS, PREC, U, MINB>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
         attr_set |= 1u << dev;
     }
     const uint64_t grid = uint64_t(a.n_wblocks) * a.n_slices;
     if (grid == 0) return ACCSPMM_SUCCESS;
     if (grid > 0x7FFFFFFFull) ACC_FAIL(ACCSPMM_ERROR_OVERFLOW, "grid too large");
-    spmm_window_kernel<FS, PREC><<<unsigned(grid), kNW * 32, smem, s>>>(a);
+    spmm_window_kernel<FS, PREC, U, MINB><<<unsigned(grid), kNW * 32, smem, s>>>(a);
     ACC_LAUNCH_CHECK();
     return ACCSPMM_SUCCESS;
+}
+
+// occ = 2: the batch of DirectBatch (64 floats of B per lane in flight) at 2
+// CTAs per SM; occ = 3: half that batch at 3 CTAs per SM (80 registers a
+// thread), which keeps more warps' gathers in flight per SM.
+template <int FS, int PREC>
+int launch_direct(const SpmmArgs& a, int occ, cudaStream_t s) {
+    if (occ == 3) return launch_direct_t<FS, PREC, (DirectBatch<FS>::U + 1) / 2, 3>(a, s);
+    return launch_direct_t<FS, PREC, DirectBatch<FS>::U, 2>(a, s);
 }
 
 }  // namespace
@@ -355,10 +370,11 @@ int spmm_window_launch(const uint32_t* rwo, const uint32_t* tc_offset, const uin
         }
     }
     const bool x3 = precision == ACCSPMM_PREC_3XTF32;
+    const int occ = cfg.occ;
     switch (cfg.fs) {
-        case 32: return x3 ? launch_direct<32, ACCSPMM_PREC_3XTF32>(a, s) : launch_direct<32, ACCSPMM_PREC_TF32>(a, s);
-        case 64: return x3 ? launch_direct<64, ACCSPMM_PREC_3XTF32>(a, s) : launch_direct<64, ACCSPMM_PREC_TF32>(a, s);
-        default: return x3 ? launch_direct<128, ACCSPMM_PREC_3XTF32>(a, s) : launch_direct<128, ACCSPMM_PREC_TF32>(a, s);
+        case 32: return x3 ? launch_direct<32, ACCSPMM_PREC_3XTF32>(a, occ, s) : launch_direct<32, ACCSPMM_PREC_TF32>(a, occ, s);
+        case 64: return x3 ? launch_direct<64, ACCSPMM_PREC_3XTF32>(a, occ, s) : launch_direct<64, ACCSPMM_PREC_TF32>(a, occ, s);
+        default: return x3 ? launch_direct<128, ACCSPMM_PREC_3XTF32>(a, occ, s) : launch_direct<128, ACCSPMM_PREC_TF32>(a, occ, s);
     }
 }
 
@@ -404,9 +420,10 @@ int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uin
 
 // ---------------------------------------------------------------------------
 // Allocation-free adaptive SpMM.  Callers that may not allocate device memory
-// -- code running while a CUDA graph is being captured into a pool they do
-// not own, real-time loops that forbid allocator calls, hosts whose memory
-// budget is fixed up front -- use this variant: its only scratch (the
+// -- plugins inside a host application that owns all device memory through
+// its own pool, latency-critical loops in which cudaFree's device-wide
+// synchronisation would stall other streams, processes whose memory budget
+// is fixed at start-up -- use this variant: its only scratch (the
 // rowWindowOffset derived from rowIndices plus a status word) lives in the
 // file-scope array below, which every GPU that loads the library holds until
 // the process exits.  All calls share the array, so calls that overlap on the
@@ -478,12 +495,15 @@ int autotune_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K
     }
     const Config dflt = choose_config(m->num_windows, m->num_tiles, K, precision);
     std::vector<Config> cand;
-    for (int kernel : {int(kDirect), int(kDb)})
+    // (kernel, CTAs per SM): register-direct at 3 and 2, double-buffered at 2
+    const int shapes[3][2] = {{kDirect, 3}, {kDirect, 2}, {kDb, 2}};
+    for (const auto& ko : shapes)
         for (int fs : {32, 64, 128}) {
             if (fs > 32 && uint32_t(fs / 2) >= K) continue;  // slices far wider than K
             for (uint32_t wb : {4u, 8u, 16u, 32u}) {
                 Config c = dflt;
-                c.kernel = kernel;
+                c.kernel = ko[0];
+                c.occ = ko[1];
                 c.fs = fs;
                 c.wb = wb;
                 c.slice_major = 0;
@@ -531,6 +551,7 @@ int autotune_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K
     }
     if (out) {
         out->kernel = best.kernel;
+        out->ctas_per_sm = best.kernel == kDirect ? uint32_t(best.occ) : 2u;
         out->slice_width = uint32_t(best.fs);
         out->windows_per_cta = best.wb;
         out->best_ms = best_ms;

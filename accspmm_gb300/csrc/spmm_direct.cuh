@@ -17,12 +17,17 @@ __device__ __forceinline__ uint64_t shfl_u64(uint64_t v, int src) {
 // Register-direct SpMM of one work item (window block, feature slice) by one
 // CTA: each lane loads its B fragments straight from global memory, a batch
 // of U tiles at a time.  `blk` must be initialised for the item.
-template <int FS, int PREC>
+// Default batch: 64 floats of B fragments per lane in flight.
+template <int FS>
+struct DirectBatch {
+    static constexpr int U = FS >= 128 ? 2 : (FS == 64 ? 4 : 8);
+};
+
+template <int FS, int PREC, int U = DirectBatch<FS>::U>
 __device__ __forceinline__ void direct_item(const SpmmArgs& a, const Block<FS, kDirectNW>& blk) {
     constexpr int H = FS / 32;
     using L = Layout<H>;
     constexpr int NM = L::NM;
-    constexpr int U = H >= 4 ? 2 : (H == 2 ? 4 : 8);  // tiles per batch
     constexpr int MA = (8 * U + 31) / 32;             // a2b registers per lane
 
     const int lane = blk.lane, g = blk.g, tq = blk.tq;

@@ -211,10 +211,12 @@ int accspmm_spmm_adaptive(const accspmm_adpbme_t* adp, const float* B,
                           int32_t precision, void* stream);
 
 /* Allocation-free variant of accspmm_spmm_adaptive, for callers that cannot
- * allocate device memory at call time: work issued while a CUDA graph is
- * captured into a memory pool the caller does not own, real-time loops that
- * forbid allocator calls, or hosts whose device memory is budgeted up front.
- * No counterpart in the reference.  It calls no cudaMalloc, cudaFree or other
+ * allocate device memory at call time: plugins inside a host application
+ * that owns all device memory through its own pool (a cudaMalloc outside
+ * that pool can fail once the pool holds the memory, and escapes the host's
+ * accounting), latency-critical loops (cudaFree synchronises the device and
+ * stalls every other stream), and processes whose device memory is budgeted
+ * once at start-up.  No counterpart in the reference.  It calls no cudaMalloc, cudaFree or other
  * allocating routine: its scratch (the row-window offsets derived from
  * rowIndices, 4 (c_rows / 8 + 2) bytes) lives in a 4 MiB array compiled into
  * the library, which every GPU that loads the library holds until the
@@ -241,9 +243,9 @@ int accspmm_time_spmm(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp,
 /* ---- autotuning ----------------------------------------------------------- */
 /* No counterpart in the reference (its launch shape is fixed: warps = K/32 or
  * K/64 per CTA, one CTA per window or group).  Times the candidate launch
- * shapes -- kernel variant (register-direct, double-buffered), feature-slice
- * width (32/64/128 columns) and windows per CTA (4/8/16/32, the load-balance
- * granularity) -- on this matrix with this B, and keeps the fastest for the
+ * shapes -- kernel variant (register-direct at 3 or 2 CTAs per SM,
+ * double-buffered), feature-slice width (32/64/128 columns) and windows per
+ * CTA (4/8/16/32, the load-balance granularity) -- on this matrix with this B, and keeps the fastest for the
  * matrix's signature (windows, tiles, K, precision) for the rest of the
  * process: later plain, adaptive and batched calls on a matrix with that
  * signature use it.  C is overwritten.  Results of different shapes agree
@@ -256,6 +258,7 @@ typedef struct accspmm_tune_result {
     float best_ms;             /* time of the chosen shape */
     float default_ms;          /* time of the default shape */
     uint32_t candidates;
+    uint32_t ctas_per_sm;      /* resident CTAs per SM of the chosen kernel */
 } accspmm_tune_result_t;
 
 int accspmm_autotune_metcf(const accspmm_metcf_t* metcf, const float* B, float* C,

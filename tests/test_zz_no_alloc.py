@@ -1,8 +1,10 @@
 """The allocation-free adaptive SpMM entry point.
 
-Some callers cannot allocate device memory when they call the library (work
-captured into a CUDA graph whose memory pool they do not own, loops that must
-not touch the allocator, fixed device-memory budgets).  For them
+Some callers cannot allocate device memory when they call the library:
+plugins inside a host application that owns all device memory through its own
+pool, latency-critical loops in which cudaFree's device-wide synchronisation
+would stall other streams, and processes with a device-memory budget fixed at
+start-up.  For them
 accspmm_spmm_adaptive_noalloc keeps its scratch in an array compiled into the
 library.  These tests call it through the C ABI and check that it returns
 what accspmm_spmm_adaptive returns, on two calls in a row (the shared scratch
