@@ -15,6 +15,7 @@ objects with a `data_ptr()` (torch tensors) or raw integer addresses.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -103,6 +104,19 @@ def metcf_struct(m: dict) -> _Keep:
     return _Keep(s, rwo, tco, bits, a2b, d)
 
 
+def adpbme_struct(a: dict) -> _Keep:
+    go = np.ascontiguousarray(a["group_offset"], np.uint32)
+    tco = np.ascontiguousarray(a["tc_offset"], np.uint32)
+    ri = np.ascontiguousarray(a["row_indices"], np.uint32)
+    bits = np.ascontiguousarray(a["bits"], np.uint64)
+    a2b = np.ascontiguousarray(a["a2b"], np.uint32)
+    d = np.ascontiguousarray(a["data"], np.float32)
+    s = ADPBME(a["rows"], a["cols"], a["nnz"], len(bits), len(go) - 1, _ptr(go, C.c_uint32),
+               _ptr(tco, C.c_uint32), _ptr(ri, C.c_uint32), _ptr(bits, C.c_uint64),
+               _ptr(a2b, C.c_uint32), _ptr(d, C.c_float), capi.HOST, 0)
+    return _Keep(s, go, tco, ri, bits, a2b, d)
+
+
 def csr_from_coo(rows, cols, row, col, data) -> dict:
     k = coo_struct(rows, cols, row, col, data)
     out = CSR()
@@ -151,6 +165,36 @@ def adpbme_from_metcf(m: dict, t_load=3, t_comp=1, t_write=2, target_num=16) -> 
     out = ADPBME()
     call("accspmm_adpbme_from_metcf", C.byref(k.struct), t_load, t_comp, t_write, target_num,
          C.byref(out), None)
+    res = adpbme_to_numpy(out)
+    load().accspmm_adpbme_destroy(C.byref(out))
+    return res
+
+
+def save_metcf(m: dict, path: str) -> None:
+    """Writes a host METCF (dict of arrays) to a binary file."""
+    k = metcf_struct(m)
+    call("accspmm_metcf_save", C.byref(k.struct), os.fsencode(path), None)
+
+
+def load_metcf(path: str) -> dict:
+    """Reads and validates a binary METCF file into host arrays."""
+    out = METCF()
+    call("accspmm_metcf_load", os.fsencode(path), capi.HOST, C.byref(out), None)
+    res = metcf_to_numpy(out)
+    load().accspmm_metcf_destroy(C.byref(out))
+    return res
+
+
+def save_adpbme(a: dict, path: str) -> None:
+    """Writes a host AdpBME (dict of arrays) to a binary file."""
+    k = adpbme_struct(a)
+    call("accspmm_adpbme_save", C.byref(k.struct), os.fsencode(path), None)
+
+
+def load_adpbme(path: str) -> dict:
+    """Reads and validates a binary AdpBME file into host arrays."""
+    out = ADPBME()
+    call("accspmm_adpbme_load", os.fsencode(path), capi.HOST, C.byref(out), None)
     res = adpbme_to_numpy(out)
     load().accspmm_adpbme_destroy(C.byref(out))
     return res
@@ -217,6 +261,16 @@ class DeviceMETCF(DeviceObject):
         call("accspmm_metcf_copy", C.byref(k.struct), capi.DEVICE, C.byref(out), _stream(stream))
         _sync(stream)
         return cls(out)
+
+    @classmethod
+    def load(cls, path: str, stream=None) -> "DeviceMETCF":
+        """Reads and validates a binary METCF file straight into device memory."""
+        out = METCF()
+        call("accspmm_metcf_load", os.fsencode(path), capi.DEVICE, C.byref(out), _stream(stream))
+        return cls(out)
+
+    def save(self, path: str, stream=None) -> None:
+        call("accspmm_metcf_save", self.ref, os.fsencode(path), _stream(stream))
 
     @classmethod
     def from_csr(cls, dcsr: DeviceCSR, stream=None) -> "DeviceMETCF":

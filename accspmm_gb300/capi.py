@@ -23,6 +23,7 @@ f32p = C.POINTER(C.c_float)
 vp = C.c_void_p
 
 SUCCESS = 0
+ERROR_OPEN_FILE = 2
 ERROR_READ_MTX = 3
 ERROR_ARGS = 4
 MM_LOADING_FILE_ERROR = -1
@@ -35,6 +36,7 @@ ERROR_OVERFLOW = 34
 ERROR_TIMEOUT = 35
 ERROR_ADMISSION = 36
 ERROR_CANCELLED = 37
+ERROR_FORMAT = 38
 PREC_TF32 = 0
 PREC_3XTF32 = 1
 HOST = 0
@@ -101,6 +103,10 @@ _SIGS = {
     "accspmm_csr_copy": ([C.POINTER(CSR), i32, C.POINTER(CSR), vp], C.c_int),
     "accspmm_coo_copy": ([C.POINTER(COO), i32, C.POINTER(COO), vp], C.c_int),
     "accspmm_adpbme_copy": ([C.POINTER(ADPBME), i32, C.POINTER(ADPBME), vp], C.c_int),
+    "accspmm_metcf_save": ([C.POINTER(METCF), C.c_char_p, vp], C.c_int),
+    "accspmm_metcf_load": ([C.c_char_p, i32, C.POINTER(METCF), vp], C.c_int),
+    "accspmm_adpbme_save": ([C.POINTER(ADPBME), C.c_char_p, vp], C.c_int),
+    "accspmm_adpbme_load": ([C.c_char_p, i32, C.POINTER(ADPBME), vp], C.c_int),
     "accspmm_coo_destroy": ([C.POINTER(COO)], None),
     "accspmm_csr_destroy": ([C.POINTER(CSR)], None),
     "accspmm_metcf_destroy": ([C.POINTER(METCF)], None),

@@ -267,6 +267,30 @@ int accspmm_adpbme_copy(const accspmm_adpbme_t* src, int32_t dst_space, accspmm_
     return ACCSPMM_SUCCESS;
 }
 
+int accspmm_metcf_save(const accspmm_metcf_t* metcf, const char* path, void* stream) {
+    clear_error();
+    if (!metcf || !path || !valid_space(metcf->space)) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "bad argument");
+    return metcf_save(metcf, path, stream);
+}
+
+int accspmm_metcf_load(const char* path, int32_t space, accspmm_metcf_t* metcf, void* stream) {
+    clear_error();
+    if (!path || !metcf || !valid_space(space)) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "bad argument");
+    return metcf_load(path, space, metcf, stream);
+}
+
+int accspmm_adpbme_save(const accspmm_adpbme_t* adp, const char* path, void* stream) {
+    clear_error();
+    if (!adp || !path || !valid_space(adp->space)) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "bad argument");
+    return adpbme_save(adp, path, stream);
+}
+
+int accspmm_adpbme_load(const char* path, int32_t space, accspmm_adpbme_t* adp, void* stream) {
+    clear_error();
+    if (!path || !adp || !valid_space(space)) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "bad argument");
+    return adpbme_load(path, space, adp, stream);
+}
+
 void accspmm_coo_destroy(accspmm_coo_t* c) {
     if (!c || !c->owned) return;
     free_in(c->space, c->row);

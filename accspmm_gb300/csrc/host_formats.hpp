@@ -17,6 +17,12 @@ int adpbme_from_metcf_host(const accspmm_metcf_t* m, uint32_t t_load, uint32_t t
                            uint32_t t_write, uint32_t target_num, accspmm_adpbme_t* a);
 int balance_strategy_host(const uint32_t* rwo, uint32_t W, uint32_t T);
 
+// binary files (metcf_io.cpp)
+int metcf_save(const accspmm_metcf_t* m, const char* path, void* stream);
+int metcf_load(const char* path, int32_t space, accspmm_metcf_t* out, void* stream);
+int adpbme_save(const accspmm_adpbme_t* a, const char* path, void* stream);
+int adpbme_load(const char* path, int32_t space, accspmm_adpbme_t* out, void* stream);
+
 // device builders (metcf_device.cu)
 int csr_from_coo_device(const accspmm_coo_t* coo, accspmm_csr_t* csr, void* stream);
 int metcf_from_csr_device(const accspmm_csr_t* csr, accspmm_metcf_t* out, void* stream);

@@ -10,7 +10,11 @@
 // Extra options, after the two positional arguments:
 //   --precision tf32|3xtf32   arithmetic (default tf32)
 //   --host-build              build METCF / AdpBME on the host instead
+//   --metcf-cache             load METCF from <matrix.mtx>.metcf when that
+//                             file is newer than the .mtx; otherwise build it
+//                             and write the file for the next run
 #include <cuda_runtime.h>
+#include <sys/stat.h>
 
 #include <cstdio>
 #include <cstdlib>
@@ -27,6 +31,13 @@ static std::string base_name(const std::string& s) {
     return p == std::string::npos ? s : s.substr(p + 1);
 }
 
+// modification time, or -1 if the file does not exist
+static long long mtime_of(const std::string& path) {
+    struct stat sb;
+    if (stat(path.c_str(), &sb) != 0) return -1;
+    return (long long)sb.st_mtime;
+}
+
 static int fail(const char* what, int st) {
     std::fprintf(stderr, "mma: %s failed (status %d): %s\n", what, st, accspmm_last_error());
     return 1;
@@ -41,11 +52,14 @@ int main(int argc, char** argv) {
     const int feature_dim = std::atoi(argv[2]);
     int precision = ACCSPMM_PREC_TF32;
     bool host_build = false;
+    bool metcf_cache = false;
     for (int i = 3; i < argc; ++i) {
         if (!std::strcmp(argv[i], "--precision") && i + 1 < argc) {
             precision = !std::strcmp(argv[++i], "3xtf32") ? ACCSPMM_PREC_3XTF32 : ACCSPMM_PREC_TF32;
         } else if (!std::strcmp(argv[i], "--host-build")) {
             host_build = true;
+        } else if (!std::strcmp(argv[i], "--metcf-cache")) {
+            metcf_cache = true;
         }
     }
     if (feature_dim <= 0 || feature_dim % 4) {
@@ -55,34 +69,46 @@ int main(int argc, char** argv) {
     const uint32_t K = uint32_t(feature_dim);
     const std::string mtx_name = base_name(filename);
 
-    accspmm_coo_t coo;
-    int st = accspmm_read_mtx(filename, &coo);
-    if (st != ACCSPMM_SUCCESS) {
-        std::fprintf(stderr, "mma: %s\n", accspmm_last_error());
-        return ACCSPMM_ERROR_READ_MTX;
-    }
-    std::cout << "m_tmp: " << coo.rows << ", n_tmp: " << coo.cols << ", nnz_tmp: " << coo.nnz << std::endl;
     cudaStream_t s;
     cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-
-    accspmm_csr_t csr;
-    if ((st = accspmm_csr_from_coo(&coo, &csr, s))) return fail("csr_from_coo", st);
-    const uint32_t num_edges = coo.nnz;
-    accspmm_coo_destroy(&coo);
-
+    const std::string cache_path = std::string(filename) + ".metcf";
     accspmm_metcf_t m;
-    if (host_build) {
-        accspmm_metcf_t hm;
-        if ((st = accspmm_metcf_from_csr(&csr, &hm, s))) return fail("metcf_from_csr", st);
-        if ((st = accspmm_metcf_copy(&hm, ACCSPMM_DEVICE, &m, s))) return fail("metcf_copy", st);
-        accspmm_metcf_destroy(&hm);
-    } else {
-        accspmm_csr_t dcsr;
-        if ((st = accspmm_csr_copy(&csr, ACCSPMM_DEVICE, &dcsr, s))) return fail("csr_copy", st);
-        if ((st = accspmm_metcf_from_csr(&dcsr, &m, s))) return fail("metcf_from_csr", st);
-        accspmm_csr_destroy(&dcsr);
+    int st = 1;
+    if (metcf_cache && mtime_of(cache_path) >= mtime_of(filename) && mtime_of(filename) >= 0) {
+        st = accspmm_metcf_load(cache_path.c_str(), ACCSPMM_DEVICE, &m, s);
+        if (st) std::fprintf(stderr, "mma: ignoring %s: %s\n", cache_path.c_str(), accspmm_last_error());
+        else std::cout << "loaded " << cache_path << std::endl;
     }
-    accspmm_csr_destroy(&csr);
+    if (st) {
+        accspmm_coo_t coo;
+        st = accspmm_read_mtx(filename, &coo);
+        if (st != ACCSPMM_SUCCESS) {
+            std::fprintf(stderr, "mma: %s\n", accspmm_last_error());
+            return ACCSPMM_ERROR_READ_MTX;
+        }
+        std::cout << "m_tmp: " << coo.rows << ", n_tmp: " << coo.cols << ", nnz_tmp: " << coo.nnz << std::endl;
+
+        accspmm_csr_t csr;
+        if ((st = accspmm_csr_from_coo(&coo, &csr, s))) return fail("csr_from_coo", st);
+        accspmm_coo_destroy(&coo);
+
+        if (host_build) {
+            accspmm_metcf_t hm;
+            if ((st = accspmm_metcf_from_csr(&csr, &hm, s))) return fail("metcf_from_csr", st);
+            if ((st = accspmm_metcf_copy(&hm, ACCSPMM_DEVICE, &m, s))) return fail("metcf_copy", st);
+            accspmm_metcf_destroy(&hm);
+        } else {
+            accspmm_csr_t dcsr;
+            if ((st = accspmm_csr_copy(&csr, ACCSPMM_DEVICE, &dcsr, s))) return fail("csr_copy", st);
+            if ((st = accspmm_metcf_from_csr(&dcsr, &m, s))) return fail("metcf_from_csr", st);
+            accspmm_csr_destroy(&dcsr);
+        }
+        accspmm_csr_destroy(&csr);
+        if (metcf_cache && (st = accspmm_metcf_save(&m, cache_path.c_str(), s)))
+            std::fprintf(stderr, "mma: could not write %s: %s\n", cache_path.c_str(), accspmm_last_error());
+    }
+    // nnz after symmetric expansion: the METCF holds exactly the CSR's values
+    const uint32_t num_edges = m.nnz;
 
     int adaptive = 0;
     if ((st = accspmm_balance_strategy(&m, &adaptive, s))) return fail("balance_strategy", st);

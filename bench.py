@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--no-sweep", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-host-build", action="store_true")
+    p.add_argument("--no-cusparse", action="store_true",
+                   help="skip the cuSPARSE CSR SpMM comparator (torch.sparse, FP32)")
     p.add_argument("--no-autotune", action="store_true",
                    help="time the default launch shape instead of the autotuned one")
     p.add_argument("--workload", default="scale", choices=["scale", "batch", "precision", "serve"],
@@ -169,6 +171,38 @@ def measured_traffic(K):
     except OSError:
         pass
     return None
+
+
+def cusparse_comparator(rp, ci, v, B, reps=10):
+    """cuSPARSE CSR SpMM (through torch.sparse, FP32 arithmetic) on the same
+    matrix and B: the vendor library's time for the same product, reported
+    beside ours as context.  Not part of the measured path."""
+    import torch
+    dev = B.device
+    n = len(rp) - 1
+    A = torch.sparse_csr_tensor(torch.from_numpy(rp.astype(np.int32)).to(dev),
+                                torch.from_numpy(ci.astype(np.int32)).to(dev),
+                                torch.from_numpy(v).to(dev), size=(n, B.shape[0]))
+    with torch.no_grad():
+        for _ in range(3):
+            out = A.matmul(B)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            out = A.matmul(B)
+        e1.record()
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    del out, A
+    return {"ms": round(ms, 4), "gflops": round(2.0 * len(ci) * B.shape[1] / (ms * 1e-3) / 1e9, 1),
+            "what": "torch.sparse_csr_tensor @ dense B (cuSPARSE SpMM, FP32, int32 indices)"}
+
+
+def gathered_rows(m):
+    """Non-padding sparseA2B entries (B rows gathered per feature column)."""
+    a2b = m.to_numpy()["a2b"]
+    return int(np.count_nonzero(a2b != np.uint32(0xFFFFFFFF)))
 
 
 def cpu_baseline(rp, ci, v, B, budget_s=8.0):
@@ -355,24 +389,34 @@ def run_ours(args):
                 "kernel_ms": round(kms, 4), "algorithmic_bytes": int(abytes)}
     if traffic:
         roofline["dram_gbs"] = round(traffic / (kms * 1e-3) / 1e9, 1)
+    # gather model (diagnostic): B counted as one K-float row per non-padding
+    # sparseA2B entry, i.e. the bytes the kernel must move from L2/HBM to SMs
+    U = gathered_rows(m) if rank == 0 else None
+    if U is not None:
+        gbytes = abytes - 4 * n * K + 4 * K * U
+        roofline["gather_model"] = {"bytes": int(gbytes), "gathered_rows": U,
+                                    "achieved": round(gbytes / (kms * 1e-3) / 1e9, 1),
+                                    "frac": round(gbytes / (kms * 1e-3) / 1e9 / peak, 4)}
 
     # end to end through the C ABI with host buffers: B host->device, SpMM,
     # C device->host, every step
     Bh = torch.empty((n, K), dtype=torch.float32, pin_memory=True)
     Bh.copy_(B.cpu())
-    Ch = torch.empty((c_rows, K), dtype=torch.float32, pin_memory=True)
+    # the product A*B is the first 8W rows of C (the adaptive path's C is
+    # taller, its extra rows are zeros)
+    Ch = torch.empty((m.c_rows, K), dtype=torch.float32, pin_memory=True)
     Bd = torch.empty_like(B)
     e2e_steps = max(3, min(args.steps, 10))
     for _ in range(2):
         Bd.copy_(Bh, non_blocking=True)
         step(Bd, C)
-        Ch.copy_(C, non_blocking=True)
+        Ch.copy_(C[:m.c_rows], non_blocking=True)
     torch.cuda.synchronize()
     e0.record(stream)
     for _ in range(e2e_steps):
         Bd.copy_(Bh, non_blocking=True)
         step(Bd, C)
-        Ch.copy_(C, non_blocking=True)
+        Ch.copy_(C[:m.c_rows], non_blocking=True)
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / e2e_steps
@@ -398,6 +442,9 @@ def run_ours(args):
                               "gbs_algorithmic": round(algorithmic_bytes(nnz, T, W, n, kk) / (kt * 1e-3) / 1e9, 1)}
             del Bk, Ck
 
+    cusparse = None
+    if not args.no_cusparse and rank == 0:
+        cusparse = cusparse_comparator(rp, ci, vals, B)
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -426,6 +473,7 @@ def run_ours(args):
         "gpu_launches": args.steps * launches_per_step,
         "clocks": clk.summary(),
         "k_sweep": sweep,
+        "comparators": {"cusparse_csr": cusparse},
     }
     print(json.dumps(out))
     if world > 1:

@@ -63,7 +63,8 @@ enum {
     ACCSPMM_ERROR_OVERFLOW = 34,
     ACCSPMM_ERROR_TIMEOUT = 35,
     ACCSPMM_ERROR_ADMISSION = 36,
-    ACCSPMM_ERROR_CANCELLED = 37
+    ACCSPMM_ERROR_CANCELLED = 37,
+    ACCSPMM_ERROR_FORMAT = 38  /* a binary METCF / AdpBME file is invalid */
 };
 
 /* arithmetic of the SpMM */
@@ -185,6 +186,24 @@ int accspmm_coo_copy(const accspmm_coo_t* src, int32_t dst_space,
                      accspmm_coo_t* dst, void* stream);
 int accspmm_adpbme_copy(const accspmm_adpbme_t* src, int32_t dst_space,
                         accspmm_adpbme_t* dst, void* stream);
+
+/* Binary METCF / AdpBME files.  No counterpart in the reference, which
+ * re-parses the .mtx text and rebuilds METCF on every run
+ * (src/mma_tf32.cu:196-222).  A file holds the struct's sizes and arrays, each
+ * with a 64-bit checksum; little-endian hosts only.  *_save accepts a host or
+ * device object (a device one is copied to the host first).  *_load reads
+ * into `space` (a library-owned object; release it with *_destroy) and
+ * validates the arrays -- offsets monotone and matching the sizes, bitmap
+ * popcounts no larger than the per-tile value counts, columns in range or padding
+ * -- so that a damaged file returns ACCSPMM_ERROR_FORMAT (truncation, wrong
+ * magic or version, checksum or consistency failure) instead of reaching a
+ * kernel.  ACCSPMM_ERROR_OPEN_FILE if the file cannot be opened or written. */
+int accspmm_metcf_save(const accspmm_metcf_t* metcf, const char* path, void* stream);
+int accspmm_metcf_load(const char* path, int32_t space, accspmm_metcf_t* metcf,
+                       void* stream);
+int accspmm_adpbme_save(const accspmm_adpbme_t* adp, const char* path, void* stream);
+int accspmm_adpbme_load(const char* path, int32_t space, accspmm_adpbme_t* adp,
+                        void* stream);
 
 void accspmm_coo_destroy(accspmm_coo_t* coo);
 void accspmm_csr_destroy(accspmm_csr_t* csr);

@@ -45,3 +45,25 @@ def test_full_run_appends_result_line(tmp_path, name, k):
     assert float(fields[2]) > 0 and float(fields[3]) > 0
     r = run([path, str(k), "--precision", "3xtf32", "--host-build"], tmp_path)
     assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.gpu
+def test_metcf_cache_is_written_then_reused(tmp_path):
+    import shutil
+
+    import numpy as np
+
+    from accspmm_gb300 import api
+    from tests.helpers import gold
+    mtx = str(tmp_path / "g.mtx")
+    shutil.copy(os.path.join(GOLD, "inputs", "plsym1000.mtx"), mtx)
+    r = run([mtx, "64", "--metcf-cache"], tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert "m_tmp" in r.stdout and os.path.exists(mtx + ".metcf")
+    back = api.load_metcf(mtx + ".metcf")
+    np.testing.assert_array_equal(back["a2b"], gold("plsym1000")["m_a2b"])
+    r = run([mtx, "64", "--metcf-cache"], tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert "loaded" in r.stdout and "m_tmp" not in r.stdout
+    a, b = (tmp_path / "result.csv").read_text().splitlines()
+    assert a.split(",")[:2] == b.split(",")[:2]
