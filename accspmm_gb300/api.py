@@ -40,6 +40,8 @@ def _addr(x) -> int:
         return 0
     if hasattr(x, "data_ptr"):
         return int(x.data_ptr())
+    if isinstance(x, np.ndarray):
+        return int(x.ctypes.data)
     return int(x)
 
 
@@ -304,6 +306,27 @@ class DeviceMETCF(DeviceObject):
         call("accspmm_spmm_tf32", self.ref, C.c_void_p(_addr(B)), C.c_void_p(_addr(C_out)), K,
              precision, _stream(stream))
 
+    def spmm_bias_act(self, B, C_out, K: int, bias=None, activation: int = capi.ACT_NONE,
+                      precision: int = capi.PREC_TF32, stream=None) -> None:
+        """C_out = act(A * B + bias) with the epilogue fused into the C store."""
+        call("accspmm_spmm_bias_act", self.ref, C.c_void_p(_addr(B)), C.c_void_p(_addr(C_out)), K,
+             precision, C.c_void_p(_addr(bias)), activation, _stream(stream))
+
+    def gcn_layer(self, H, k_in: int, W, k_out: int, out, bias=None,
+                  activation: int = capi.ACT_RELU, precision: int = capi.PREC_TF32,
+                  stream=None) -> None:
+        """out = act(A * (H W) + bias): cuBLAS for H W, the fused SpMM for A."""
+        call("accspmm_gcn_layer", self.ref, C.c_void_p(_addr(H)), k_in, C.c_void_p(_addr(W)),
+             k_out, C.c_void_p(_addr(bias)), activation, C.c_void_p(_addr(out)), precision,
+             _stream(stream))
+
+    def spmm_host(self, B_host, C_host, K: int, precision: int = capi.PREC_TF32, stream=None) -> None:
+        """C_host = A * B_host with both dense matrices in host memory
+        (accspmm_spmm_host); C_host has 8 ceil(rows / 8) rows.  Complete when
+        `stream` is."""
+        call("accspmm_spmm_host", self.ref, None, C.c_void_p(_addr(B_host)),
+             C.c_void_p(_addr(C_host)), K, precision, _stream(stream))
+
     def autotune(self, B, C_out, K: int, precision: int = capi.PREC_TF32, stream=None) -> dict:
         """Times the candidate launch shapes and keeps the fastest for this
         matrix's signature (overwrites C_out)."""
@@ -330,6 +353,12 @@ class DeviceADPBME(DeviceObject):
         v = C.c_uint32(0)
         call("accspmm_adaptive_c_rows", self.ref, C.byref(v), _stream(stream))
         return v.value
+
+    def spmm_host(self, B_host, C_host, K: int, precision: int = capi.PREC_TF32, stream=None) -> None:
+        """Adaptive-path C_host = A * B_host from host memory
+        (accspmm_spmm_host); C_host has 8 ceil(rows / 8) rows."""
+        call("accspmm_spmm_host", None, self.ref, C.c_void_p(_addr(B_host)),
+             C.c_void_p(_addr(C_host)), K, precision, _stream(stream))
 
     def spmm(self, B, C_out, c_rows: int, K: int, precision: int = capi.PREC_TF32,
              stream=None) -> None:

@@ -25,7 +25,7 @@ LIB = os.path.join(PKG, "libaccspmm.so")
 CLI = os.path.join(PKG, "bin", "mma")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-LIB_UNITS = ["host_formats.cpp", "metcf_io.cpp", "capi.cpp", "device_prims.cu", "metcf_device.cu", "spmm.cu", "spmm_pipe.cu", "spmm_bulk.cu", "spmm_lean.cu", "spmm_batch.cu", "server.cpp"]
+LIB_UNITS = ["host_formats.cpp", "metcf_io.cpp", "capi.cpp", "device_prims.cu", "metcf_device.cu", "spmm.cu", "spmm_host.cpp", "spmm_pipe.cu", "spmm_bulk.cu", "spmm_lean.cu", "spmm_batch.cu", "server.cpp", "gnn.cpp"]
 
 
 def cuda_home() -> str:
@@ -78,7 +78,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
     nvcc = os.path.join(cuda, "bin", "nvcc")
     lib_objs = objs[:-1]
     if force or _stale(LIB, lib_objs):
-        cmd = [nvcc, *ARCH, "-shared", "-cudart", "static", "-o", LIB, *lib_objs, "-lpthread"]
+        lib64 = os.path.join(cuda, "lib64")
+        cmd = [nvcc, *ARCH, "-shared", "-cudart", "static", "-o", LIB, *lib_objs, "-L" + lib64,
+               "-lcublas", "-Xlinker", "-rpath", "-Xlinker", lib64, "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

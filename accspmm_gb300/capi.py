@@ -39,6 +39,8 @@ ERROR_CANCELLED = 37
 ERROR_FORMAT = 38
 PREC_TF32 = 0
 PREC_3XTF32 = 1
+ACT_NONE = 0
+ACT_RELU = 1
 HOST = 0
 DEVICE = 1
 
@@ -129,6 +131,9 @@ _SIGS = {
     "accspmm_batch_launch_graph": ([vp, vp], C.c_int),
     "accspmm_batch_info": ([vp, u32p, u32p, u32p], C.c_int),
     "accspmm_batch_destroy": ([vp], None),
+    "accspmm_spmm_bias_act": ([C.POINTER(METCF), vp, vp, u32, i32, vp, i32, vp], C.c_int),
+    "accspmm_gcn_layer": ([C.POINTER(METCF), vp, u32, vp, u32, vp, i32, vp, i32, vp], C.c_int),
+    "accspmm_spmm_host": ([C.POINTER(METCF), C.POINTER(ADPBME), vp, vp, u32, i32, vp], C.c_int),
     "accspmm_spmm_adaptive_noalloc": ([C.POINTER(ADPBME), vp, vp, u32, u32, i32, vp], C.c_int),
     "accspmm_noalloc_max_c_rows": ([], C.c_uint32),
     "accspmm_time_spmm": ([C.POINTER(METCF), C.POINTER(ADPBME), vp, vp, u32, u32, i32, i32, i32,

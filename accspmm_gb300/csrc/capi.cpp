@@ -340,6 +340,26 @@ int accspmm_spmm_adaptive(const accspmm_adpbme_t* adp, const float* B, float* C,
     return spmm_adaptive_impl(adp, B, C, c_rows, K, precision, stream);
 }
 
+int accspmm_spmm_bias_act(const accspmm_metcf_t* metcf, const float* B, float* C, uint32_t K,
+                          int32_t precision, const float* bias, int32_t activation, void* stream) {
+    clear_error();
+    return spmm_bias_act_impl(metcf, B, C, K, precision, bias, activation, stream);
+}
+
+int accspmm_gcn_layer(const accspmm_metcf_t* adj, const float* H, uint32_t k_in, const float* W,
+                      uint32_t k_out, const float* bias, int32_t activation, float* out,
+                      int32_t precision, void* stream) {
+    clear_error();
+    return gcn_layer_impl(adj, H, k_in, W, k_out, bias, activation, out, precision, stream);
+}
+
+int accspmm_spmm_host(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp,
+                      const float* B_host, float* C_host, uint32_t K, int32_t precision,
+                      void* stream) {
+    clear_error();
+    return spmm_host_impl(metcf, adp, B_host, C_host, K, precision, stream, nullptr);
+}
+
 int accspmm_spmm_adaptive_noalloc(const accspmm_adpbme_t* adp, const float* B, float* C,
                                   uint32_t c_rows, uint32_t K, int32_t precision, void* stream) {
     clear_error();

@@ -215,6 +215,17 @@ __global__ void rwo_from_row_indices_kernel(const uint32_t* __restrict__ ri, uin
     if (w < Weff && lo < T && lo > 0 && ri[lo] < ri[lo - 1]) atomicOr(err, 2u);
 }
 
+}  // namespace
+
+int rwo_from_row_indices(const uint32_t* ri, uint32_t T, uint32_t W, uint32_t* rwo, uint32_t* err,
+                         cudaStream_t s) {
+    rwo_from_row_indices_kernel<<<(W + 1 + 255) / 256, 256, 0, s>>>(ri, T, W, rwo, err);
+    ACC_LAUNCH_CHECK();
+    return ACCSPMM_SUCCESS;
+}
+
+namespace {
+
 enum KernelKind { kDirect = 0, kPipe = 1, kBulk = 2, kLean = 3, kDb = 4 };
 
 struct Config {
@@ -343,18 +354,33 @@ uint32_t window_block_for(uint32_t w_cfg, uint32_t T, uint32_t K, int precision)
     return choose_config(w_cfg, T, K, precision).wb;
 }
 
+uint32_t slice_width_for(uint32_t w_cfg, uint32_t T, uint32_t K, int precision) {
+    return uint32_t(choose_config(w_cfg, T, K, precision).fs);
+}
+
 int spmm_window_launch(const uint32_t* rwo, const uint32_t* tc_offset, const uint64_t* bits,
                        const uint32_t* a2b, const float* vals, uint32_t W, uint32_t w_cfg,
                        uint32_t T, uint32_t cols, const float* B, float* C, uint32_t K,
                        int precision, cudaStream_t s) {
+    return spmm_window_launch_slices(rwo, tc_offset, bits, a2b, vals, W, w_cfg, T, cols, B, C, K,
+                                     precision, 0, 0xFFFFFFFFu, Epilogue{}, s);
+}
+
+int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, const uint64_t* bits,
+                              const uint32_t* a2b, const float* vals, uint32_t W, uint32_t w_cfg,
+                              uint32_t T, uint32_t cols, const float* B, float* C, uint32_t K,
+                              int precision, uint32_t slice_begin, uint32_t slice_count,
+                              const Epilogue& epi, cudaStream_t s) {
     if (W == 0) return ACCSPMM_SUCCESS;
     // the launch shape depends only on (w_cfg, T, K, precision), so every
     // entry point cuts a matrix into the same pieces and sums partial windows
     // in the same order
     Config cfg = choose_config(w_cfg, T, K, precision);
-    SpmmArgs a{rwo, tc_offset, bits, a2b, vals, B, C, W, cols, K, cfg.wb,
-               (K + uint32_t(cfg.fs) - 1) / uint32_t(cfg.fs), (W + cfg.wb - 1) / cfg.wb,
-               cfg.slice_major};
+    const uint32_t slices = (K + uint32_t(cfg.fs) - 1) / uint32_t(cfg.fs);
+    if (slice_begin >= slices) return ACCSPMM_SUCCESS;
+    slice_count = std::min(slice_count, slices - slice_begin);
+    SpmmArgs a{rwo, tc_offset, bits, a2b, vals, B, C, W, cols, K, cfg.wb, slice_count,
+               (W + cfg.wb - 1) / cfg.wb, cfg.slice_major, slice_begin, epi.bias, epi.act};
     if (cfg.kernel == kPipe) return launch_pipe(a, cfg.fs, precision, cfg.nw, cfg.hints, s);
     if (cfg.kernel == kBulk) return launch_bulk(a, cfg.fs, precision, cfg.nw, cfg.hints, s);
     if (cfg.kernel == kLean) return launch_lean(a, cfg.fs, precision, env_int("ACCSPMM_MINB", 4), s);
@@ -396,6 +422,24 @@ int spmm_tf32_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t 
     return spmm_window_launch(m->row_window_offset, m->tc_offset, m->tc_local_bit, m->sparse_a2b,
                               m->data, m->num_windows, m->num_windows, m->num_tiles, m->cols, B, C,
                               K, precision, as_stream(stream));
+}
+
+int spmm_bias_act_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K,
+                       int precision, const float* bias, int act, void* stream) {
+    if (!m || m->space != ACCSPMM_DEVICE) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "METCF must be on the device");
+    int st = check_dense(B, C, K, precision);
+    if (st) return st;
+    if (reinterpret_cast<uintptr_t>(bias) & 15u)
+        ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "bias must be 16-byte aligned");
+    if (act != ACCSPMM_ACT_NONE && act != ACCSPMM_ACT_RELU)
+        ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "unknown activation %d", act);
+    Epilogue epi;
+    epi.bias = bias;
+    epi.act = uint32_t(act);
+    return spmm_window_launch_slices(m->row_window_offset, m->tc_offset, m->tc_local_bit,
+                                     m->sparse_a2b, m->data, m->num_windows, m->num_windows,
+                                     m->num_tiles, m->cols, B, C, K, precision, 0, 0xFFFFFFFFu, epi,
+                                     as_stream(stream));
 }
 
 int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uint32_t c_rows,

@@ -24,9 +24,12 @@ struct SpmmArgs {
     uint32_t cols;         // rows of B
     uint32_t K;            // columns of B and C
     uint32_t wb;           // windows per CTA
-    uint32_t n_slices;     // feature slices of FS columns
+    uint32_t n_slices;     // feature slices of FS columns in this launch
     uint32_t n_wblocks;    // window blocks
     uint32_t slice_major;  // CTA order: every window block of slice 0 first
+    uint32_t slice0;       // first feature slice of this launch
+    const float* bias;     // epilogue: C = act(A B + bias[col]); nullptr: no bias
+    uint32_t act;          // epilogue activation: 0 none, 1 ReLU
 };
 
 // TF32 operand rounded to nearest, ties away from zero: the reference's
@@ -181,17 +184,36 @@ struct BitDecode {
     }
 };
 
+// Stores a finished 8-row block of C (rows row0 + 2tq + p, features f0 + 32h
+// + 4g .. + 3), applying the epilogue: + bias[feature], then the activation.
+// Every element of C is stored exactly once, so the epilogue is applied once.
 template <int FS>
-__device__ __forceinline__ void store_rows(float* __restrict__ C, uint32_t K, uint32_t row0,
-                                           uint32_t f0, int g, int tq,
-                                           const float4 (&out)[2][FS / 32]) {
+__device__ __forceinline__ void store_rows(const SpmmArgs& a, uint32_t row0, uint32_t f0, int g,
+                                           int tq, float4 (&out)[2][FS / 32]) {
+    if (a.bias || a.act) {
+#pragma unroll
+        for (int h = 0; h < FS / 32; ++h) {
+            const uint32_t f = f0 + 32 * h + 4 * g;
+            float4 b = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (a.bias && f < a.K) b = *reinterpret_cast<const float4*>(a.bias + f);
+#pragma unroll
+            for (int p = 0; p < 2; ++p) {
+                float4& v = out[p][h];
+                v.x += b.x; v.y += b.y; v.z += b.z; v.w += b.w;
+                if (a.act == ACCSPMM_ACT_RELU) {
+                    v.x = fmaxf(v.x, 0.f); v.y = fmaxf(v.y, 0.f);
+                    v.z = fmaxf(v.z, 0.f); v.w = fmaxf(v.w, 0.f);
+                }
+            }
+        }
+    }
 #pragma unroll
     for (int p = 0; p < 2; ++p) {
-        float* rowp = C + size_t(row0 + 2 * tq + p) * K;
+        float* rowp = a.C + size_t(row0 + 2 * tq + p) * a.K;
 #pragma unroll
         for (int h = 0; h < FS / 32; ++h) {
             uint32_t f = f0 + 32 * h + 4 * g;
-            if (f < K) __stcs(reinterpret_cast<float4*>(rowp + f), out[p][h]);
+            if (f < a.K) __stcs(reinterpret_cast<float4*>(rowp + f), out[p][h]);
         }
     }
 }
@@ -226,7 +248,7 @@ struct Block {
         w0 = wbk * a.wb;
         const uint32_t w1 = min(w0 + a.wb, a.W);
         nwin = w1 - w0;
-        f0 = slice * FS;
+        f0 = (a.slice0 + slice) * FS;
         for (uint32_t i = threadIdx.x; i <= nwin; i += blockDim.x) s_rwo_mem[i] = a.rwo[w0 + i];
         __syncthreads();
         s_rwo = s_rwo_mem;
@@ -269,7 +291,7 @@ struct Block {
 #pragma unroll
             for (int h = 0; h < H; ++h) out[p][h] = Layout<H>::get(acc, p, h);
         if (rb >= tb && re <= te) {
-            store_rows<FS>(a.C, a.K, (w0 + wloc) * kWin, f0, g, tq, out);
+            store_rows<FS>(a, (w0 + wloc) * kWin, f0, g, tq, out);
         } else {
             float* sp = slot(2 * warp + (is_first ? 0 : 1));
 #pragma unroll
@@ -312,7 +334,7 @@ struct Block {
                         }
                 }
             }
-            store_rows<FS>(a.C, a.K, (w0 + wloc) * kWin, f0, g, tq, out);
+            store_rows<FS>(a, (w0 + wloc) * kWin, f0, g, tq, out);
         }
     }
 };

@@ -20,6 +20,35 @@ int spmm_window_launch(const uint32_t* rwo, const uint32_t* tc_offset, const uin
                        const uint32_t* a2b, const float* vals, uint32_t W, uint32_t w_cfg,
                        uint32_t T, uint32_t cols, const float* B, float* C, uint32_t K,
                        int precision, cudaStream_t s);
+// Epilogue applied when C is stored: C = act(A B + bias[col]).
+struct Epilogue {
+    const float* bias = nullptr;  // K floats on the device, 16-byte aligned, or nullptr
+    uint32_t act = 0;             // ACCSPMM_ACT_NONE / ACCSPMM_ACT_RELU
+};
+
+// The same launch restricted to feature slices [slice_begin, slice_begin +
+// slice_count) of the chosen slice width: identical arithmetic for the
+// columns it covers.
+int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, const uint64_t* bits,
+                              const uint32_t* a2b, const float* vals, uint32_t W, uint32_t w_cfg,
+                              uint32_t T, uint32_t cols, const float* B, float* C, uint32_t K,
+                              int precision, uint32_t slice_begin, uint32_t slice_count,
+                              const Epilogue& epi, cudaStream_t s);
+// Feature columns per slice the launch-shape chooser picks.
+uint32_t slice_width_for(uint32_t w_cfg, uint32_t T, uint32_t K, int precision);
+// rowWindowOffset of W windows derived from an AdpBME's rowIndices (err: a
+// word raised when rowIndices do not fit W windows or decrease).
+int rwo_from_row_indices(const uint32_t* ri, uint32_t T, uint32_t W, uint32_t* rwo, uint32_t* err,
+                         cudaStream_t s);
+int spmm_host_impl(const accspmm_metcf_t* m, const accspmm_adpbme_t* ad, const float* B_host,
+                   float* C_host, uint32_t K, int precision, void* stream, int* direct_c);
+int spmm_bias_act_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K,
+                       int precision, const float* bias, int act, void* stream);
+int gcn_layer_impl(const accspmm_metcf_t* adj, const float* H, uint32_t k_in, const float* W,
+                   uint32_t k_out, const float* bias, int act, float* out, int precision,
+                   void* stream);
+// Per-device memory pool of the library (keeps freed memory for later calls).
+int library_pool(cudaMemPool_t* pool);
 int autotune_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K, int precision,
                   void* stream, accspmm_tune_result_t* out);
 void autotune_clear();

@@ -398,31 +398,32 @@ def run_ours(args):
                                     "achieved": round(gbytes / (kms * 1e-3) / 1e9, 1),
                                     "frac": round(gbytes / (kms * 1e-3) / 1e9 / peak, 4)}
 
-    # end to end through the C ABI with host buffers: B host->device, SpMM,
-    # C device->host, every step
+    # end to end through the C ABI with host buffers: accspmm_spmm_host takes
+    # B and C in page-locked host memory; every step copies B in (slice by
+    # slice, overlapped with the kernels) and has the kernels store A*B into
+    # host C over the host link
     Bh = torch.empty((n, K), dtype=torch.float32, pin_memory=True)
     Bh.copy_(B.cpu())
-    # the product A*B is the first 8W rows of C (the adaptive path's C is
-    # taller, its extra rows are zeros)
     Ch = torch.empty((m.c_rows, K), dtype=torch.float32, pin_memory=True)
-    Bd = torch.empty_like(B)
+    host_obj = adp if adaptive else m
+
+    def host_step():
+        host_obj.spmm_host(Bh, Ch, K, prec, stream)
+
     e2e_steps = max(3, min(args.steps, 10))
     for _ in range(2):
-        Bd.copy_(Bh, non_blocking=True)
-        step(Bd, C)
-        Ch.copy_(C[:m.c_rows], non_blocking=True)
+        host_step()
     torch.cuda.synchronize()
     e0.record(stream)
     for _ in range(e2e_steps):
-        Bd.copy_(Bh, non_blocking=True)
-        step(Bd, C)
-        Ch.copy_(C[:m.c_rows], non_blocking=True)
+        host_step()
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / e2e_steps
     e2e = {"value": round(flops * world / (e2e_ms * 1e-3) / 1e9, 2), "unit": UNIT,
            "h2d_bytes_per_step": int(Bh.numel() * 4), "d2h_bytes_per_step": int(Ch.numel() * 4),
-           "ms_per_step": round(e2e_ms, 3)}
+           "ms_per_step": round(e2e_ms, 3),
+           "api": "accspmm_spmm_host (pinned B and C; C written by the kernels over the host link)"}
 
     sweep = {}
     if not args.no_sweep and rank == 0:

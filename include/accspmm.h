@@ -73,6 +73,9 @@ enum {
     ACCSPMM_PREC_3XTF32 = 1  /* hi/lo TF32 splits of A and B, three MMAs, FP32 accumulate */
 };
 
+/* activation of the SpMM epilogue */
+enum { ACCSPMM_ACT_NONE = 0, ACCSPMM_ACT_RELU = 1 };
+
 /* memory space of an object's arrays */
 enum { ACCSPMM_HOST = 0, ACCSPMM_DEVICE = 1 };
 
@@ -228,6 +231,48 @@ int accspmm_spmm_tf32(const accspmm_metcf_t* metcf, const float* B, float* C,
 int accspmm_spmm_adaptive(const accspmm_adpbme_t* adp, const float* B,
                           float* C, uint32_t c_rows, uint32_t K,
                           int32_t precision, void* stream);
+
+/* accspmm_spmm_tf32 with an epilogue applied as C is stored:
+ * C = act(A B + bias), bias[j] added to column j (bias: K floats on the
+ * device, 16-byte aligned, or NULL), act ACCSPMM_ACT_NONE or _RELU.  Rows of
+ * C past the matrix's rows (padding of the last window) hold act(bias).
+ * Bit-identical to accspmm_spmm_tf32 followed by a separate FP32 bias add and
+ * activation.  No counterpart in the reference. */
+int accspmm_spmm_bias_act(const accspmm_metcf_t* metcf, const float* B, float* C,
+                          uint32_t K, int32_t precision, const float* bias,
+                          int32_t activation, void* stream);
+
+/* One graph-convolution layer, out = act(A (H W) + bias): H is cols x k_in,
+ * W is k_in x k_out (row-major, device), out is 8 num_windows x k_out.  H W
+ * is computed by cuBLAS (TF32 tensor cores for ACCSPMM_PREC_TF32, FP32 for
+ * ACCSPMM_PREC_3XTF32) into a buffer from the library's memory pool, then
+ * multiplied by A with the bias/activation epilogue of accspmm_spmm_bias_act.
+ * k_out must be a multiple of 4.  No counterpart in the reference. */
+int accspmm_gcn_layer(const accspmm_metcf_t* adj, const float* H, uint32_t k_in,
+                      const float* W, uint32_t k_out, const float* bias,
+                      int32_t activation, float* out, int32_t precision,
+                      void* stream);
+
+/* SpMM with B and C in host memory: the host wrappers tf32_spmm and
+ * adp_tf32_spmm, src/mma_tf32.cu:12-183 (device buffers, B copied in, one
+ * kernel, C copied out), as one pipelined call.  Pass exactly one of `metcf`
+ * (plain path) and `adp` (adaptive path), on the device.  B_host has `cols`
+ * rows and K columns; C_host receives A * B as 8 * ceil(rows / 8) rows of K
+ * columns (both paths; the adaptive path's extra zero rows are not written).
+ * The work is cut into the feature slices of the device entry points, and
+ * the host-to-device copy of slice i + 1 overlaps the kernel of slice i.
+ * When C_host is page-locked (cudaHostAlloc / cudaHostRegister) and 16-byte
+ * aligned the kernel writes C straight into it over the host link;
+ * otherwise C is staged on the device and copied back slice by slice.
+ * Page-locked B_host lets its copies run asynchronously.  Results are
+ * bit-identical to accspmm_spmm_tf32 / accspmm_spmm_adaptive on the same
+ * inputs.  Device buffers come from a library memory pool per device that
+ * keeps its memory for later calls.  Enqueued on `stream`: C_host is
+ * complete once the stream's work up to this call is done; B_host and
+ * C_host must stay valid until then. */
+int accspmm_spmm_host(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp,
+                      const float* B_host, float* C_host, uint32_t K,
+                      int32_t precision, void* stream);
 
 /* Allocation-free variant of accspmm_spmm_adaptive, for callers that cannot
  * allocate device memory at call time: plugins inside a host application
