@@ -172,6 +172,33 @@ def adpbme_from_metcf(m: dict, t_load=3, t_comp=1, t_write=2, target_num=16) -> 
     return res
 
 
+def reorder_rcm(csr: dict):
+    """Reverse Cuthill-McKee numbering of a square host CSR: (perm with
+    perm[new] = old, bandwidth before, bandwidth after)."""
+    k = csr_struct(csr)
+    perm = np.empty(csr["rows"], np.uint32)
+    b0, b1 = C.c_uint64(0), C.c_uint64(0)
+    call("accspmm_reorder_rcm", C.byref(k.struct), _ptr(perm, C.c_uint32), C.byref(b0), C.byref(b1))
+    return perm, int(b0.value), int(b1.value)
+
+
+def csr_permute(csr: dict, perm) -> dict:
+    """P A P^T of a square host CSR (A'[i, j] = A[perm[i], perm[j]])."""
+    k = csr_struct(csr)
+    p = np.ascontiguousarray(perm, np.uint32)
+    out = CSR()
+    call("accspmm_csr_permute", C.byref(k.struct), _ptr(p, C.c_uint32), C.byref(out))
+    res = csr_to_numpy(out)
+    load().accspmm_csr_destroy(C.byref(out))
+    return res
+
+
+def permute_rows(src, dst, idx, rows: int, K: int, scatter: bool = False, stream=None) -> None:
+    """Device row gather dst[i] = src[idx[i]] (or scatter dst[idx[i]] = src[i])."""
+    call("accspmm_dense_permute_rows", C.c_void_p(_addr(src)), C.c_void_p(_addr(dst)),
+         C.c_void_p(_addr(idx)), rows, K, 1 if scatter else 0, _stream(stream))
+
+
 def save_metcf(m: dict, path: str) -> None:
     """Writes a host METCF (dict of arrays) to a binary file."""
     k = metcf_struct(m)
@@ -311,6 +338,14 @@ class DeviceMETCF(DeviceObject):
         """C_out = act(A * B + bias) with the epilogue fused into the C store."""
         call("accspmm_spmm_bias_act", self.ref, C.c_void_p(_addr(B)), C.c_void_p(_addr(C_out)), K,
              precision, C.c_void_p(_addr(bias)), activation, _stream(stream))
+
+    def gather_floor(self, B, K: int, repeats: int = 10, stream=None) -> float:
+        """Milliseconds of a launch that only gathers the B rows this SpMM
+        reads (accspmm_gather_floor)."""
+        ms = C.c_float(0.0)
+        call("accspmm_gather_floor", self.ref, C.c_void_p(_addr(B)), K, repeats, C.byref(ms),
+             _stream(stream))
+        return float(ms.value)
 
     def gcn_layer(self, H, k_in: int, W, k_out: int, out, bias=None,
                   activation: int = capi.ACT_RELU, precision: int = capi.PREC_TF32,

@@ -25,7 +25,7 @@ LIB = os.path.join(PKG, "libaccspmm.so")
 CLI = os.path.join(PKG, "bin", "mma")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-LIB_UNITS = ["host_formats.cpp", "metcf_io.cpp", "capi.cpp", "device_prims.cu", "metcf_device.cu", "spmm.cu", "spmm_host.cpp", "spmm_pipe.cu", "spmm_bulk.cu", "spmm_lean.cu", "spmm_batch.cu", "server.cpp", "gnn.cpp"]
+LIB_UNITS = ["host_formats.cpp", "metcf_io.cpp", "reorder.cpp", "permute.cu", "capi.cpp", "device_prims.cu", "metcf_device.cu", "spmm.cu", "spmm_floor.cu", "spmm_host.cpp", "spmm_pipe.cu", "spmm_bulk.cu", "spmm_lean.cu", "spmm_batch.cu", "server.cpp", "gnn.cpp"]
 
 
 def cuda_home() -> str:

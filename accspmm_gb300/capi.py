@@ -105,6 +105,9 @@ _SIGS = {
     "accspmm_csr_copy": ([C.POINTER(CSR), i32, C.POINTER(CSR), vp], C.c_int),
     "accspmm_coo_copy": ([C.POINTER(COO), i32, C.POINTER(COO), vp], C.c_int),
     "accspmm_adpbme_copy": ([C.POINTER(ADPBME), i32, C.POINTER(ADPBME), vp], C.c_int),
+    "accspmm_reorder_rcm": ([C.POINTER(CSR), u32p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], C.c_int),
+    "accspmm_csr_permute": ([C.POINTER(CSR), u32p, C.POINTER(CSR)], C.c_int),
+    "accspmm_dense_permute_rows": ([vp, vp, vp, u32, u32, i32, vp], C.c_int),
     "accspmm_metcf_save": ([C.POINTER(METCF), C.c_char_p, vp], C.c_int),
     "accspmm_metcf_load": ([C.c_char_p, i32, C.POINTER(METCF), vp], C.c_int),
     "accspmm_adpbme_save": ([C.POINTER(ADPBME), C.c_char_p, vp], C.c_int),
@@ -133,6 +136,7 @@ _SIGS = {
     "accspmm_batch_destroy": ([vp], None),
     "accspmm_spmm_bias_act": ([C.POINTER(METCF), vp, vp, u32, i32, vp, i32, vp], C.c_int),
     "accspmm_gcn_layer": ([C.POINTER(METCF), vp, u32, vp, u32, vp, i32, vp, i32, vp], C.c_int),
+    "accspmm_gather_floor": ([C.POINTER(METCF), vp, u32, i32, f32p, vp], C.c_int),
     "accspmm_spmm_host": ([C.POINTER(METCF), C.POINTER(ADPBME), vp, vp, u32, i32, vp], C.c_int),
     "accspmm_spmm_adaptive_noalloc": ([C.POINTER(ADPBME), vp, vp, u32, u32, i32, vp], C.c_int),
     "accspmm_noalloc_max_c_rows": ([], C.c_uint32),

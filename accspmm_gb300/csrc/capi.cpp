@@ -267,6 +267,25 @@ int accspmm_adpbme_copy(const accspmm_adpbme_t* src, int32_t dst_space, accspmm_
     return ACCSPMM_SUCCESS;
 }
 
+int accspmm_reorder_rcm(const accspmm_csr_t* csr, uint32_t* perm, uint64_t* bandwidth_before,
+                        uint64_t* bandwidth_after) {
+    clear_error();
+    if (!csr || !perm) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "null argument");
+    return reorder_rcm_host(csr, perm, bandwidth_before, bandwidth_after);
+}
+
+int accspmm_csr_permute(const accspmm_csr_t* csr, const uint32_t* perm, accspmm_csr_t* out) {
+    clear_error();
+    if (!csr || !perm || !out) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "null argument");
+    return csr_permute_host(csr, perm, out);
+}
+
+int accspmm_dense_permute_rows(const float* src, float* dst, const uint32_t* idx, uint32_t rows,
+                               uint32_t K, int32_t scatter, void* stream) {
+    clear_error();
+    return permute_rows_impl(src, dst, idx, rows, K, scatter, stream);
+}
+
 int accspmm_metcf_save(const accspmm_metcf_t* metcf, const char* path, void* stream) {
     clear_error();
     if (!metcf || !path || !valid_space(metcf->space)) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "bad argument");
@@ -351,6 +370,12 @@ int accspmm_gcn_layer(const accspmm_metcf_t* adj, const float* H, uint32_t k_in,
                       int32_t precision, void* stream) {
     clear_error();
     return gcn_layer_impl(adj, H, k_in, W, k_out, bias, activation, out, precision, stream);
+}
+
+int accspmm_gather_floor(const accspmm_metcf_t* metcf, const float* B, uint32_t K,
+                         int32_t repeats, float* avg_ms, void* stream) {
+    clear_error();
+    return gather_floor_impl(metcf, B, K, repeats, avg_ms, stream);
 }
 
 int accspmm_spmm_host(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp,

@@ -23,6 +23,10 @@ int metcf_load(const char* path, int32_t space, accspmm_metcf_t* out, void* stre
 int adpbme_save(const accspmm_adpbme_t* a, const char* path, void* stream);
 int adpbme_load(const char* path, int32_t space, accspmm_adpbme_t* out, void* stream);
 
+// locality reordering (reorder.cpp)
+int reorder_rcm_host(const accspmm_csr_t* a, uint32_t* perm, uint64_t* bw_before, uint64_t* bw_after);
+int csr_permute_host(const accspmm_csr_t* a, const uint32_t* perm, accspmm_csr_t* out);
+
 // device builders (metcf_device.cu)
 int csr_from_coo_device(const accspmm_coo_t* coo, accspmm_csr_t* csr, void* stream);
 int metcf_from_csr_device(const accspmm_csr_t* csr, accspmm_metcf_t* out, void* stream);

@@ -46,15 +46,16 @@ __device__ __align__(16) float g_zero_row_direct[128] = {0.f};
 
 
 // One-matrix launch of the register-direct kernel: one CTA per work item.
-// U tiles per batch; MINB resident CTAs per SM (the register budget).
-template <int FS, int PREC, int U, int MINB>
+// U tiles per batch; MINB resident CTAs per SM (the register budget); EPI:
+// the bias / activation epilogue is applied as C is stored.
+template <int FS, int PREC, int U, int MINB, bool EPI>
 __global__ void __launch_bounds__(kNW * 32, MINB) spmm_window_kernel(const SpmmArgs a) {
     extern __shared__ __align__(16) float smem[];
     float* part = smem;  // [2 * kNW] slots
     uint32_t* s_rwo = reinterpret_cast<uint32_t*>(smem + 2 * kNW * 8 * FS);
     Block<FS, kNW> blk;
     blk.init(a, s_rwo, part);
-    direct_item<FS, PREC, U>(a, blk);
+    direct_item<FS, PREC, U, EPI>(a, blk);
 }
 
 // Double-buffered register-direct kernel: the gathers of batch q + 1 are
@@ -307,21 +308,21 @@ Config choose_config(uint32_t W, uint32_t T, uint32_t K, int precision) {
     return c;
 }
 
-template <int FS, int PREC, int U, int MINB>
+template <int FS, int PREC, int U, int MINB, bool EPI>
 int launch_direct_t(const SpmmArgs& a, cudaStream_t s) {
     const size_t smem = size_t(2 * kNW * 8 * FS) * 4 + size_t(a.wb + 1) * 4;
     static unsigned attr_set = 0;  // one bit per device
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 32 && !(attr_set & (1u << dev))) {
-        ACC_CUDA(cudaFuncSetAttribute(spmm_window_kernel<FS, PREC, U, MINB>,
+        ACC_CUDA(cudaFuncSetAttribute(spmm_window_kernel<FS, PREC, U, MINB, EPI>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
         attr_set |= 1u << dev;
     }
     const uint64_t grid = uint64_t(a.n_wblocks) * a.n_slices;
     if (grid == 0) return ACCSPMM_SUCCESS;
     if (grid > 0x7FFFFFFFull) ACC_FAIL(ACCSPMM_ERROR_OVERFLOW, "grid too large");
-    spmm_window_kernel<FS, PREC, U, MINB><<<unsigned(grid), kNW * 32, smem, s>>>(a);
+    spmm_window_kernel<FS, PREC, U, MINB, EPI><<<unsigned(grid), kNW * 32, smem, s>>>(a);
     ACC_LAUNCH_CHECK();
     return ACCSPMM_SUCCESS;
 }
@@ -331,8 +332,13 @@ int launch_direct_t(const SpmmArgs& a, cudaStream_t s) {
 // thread), which keeps more warps' gathers in flight per SM.
 template <int FS, int PREC>
 int launch_direct(const SpmmArgs& a, int occ, cudaStream_t s) {
-    if (occ == 3) return launch_direct_t<FS, PREC, (DirectBatch<FS>::U + 1) / 2, 3>(a, s);
-    return launch_direct_t<FS, PREC, DirectBatch<FS>::U, 2>(a, s);
+    const bool epi = a.bias != nullptr || a.act != 0;
+    if (occ == 3) {
+        constexpr int U = (DirectBatch<FS>::U + 1) / 2;
+        return epi ? launch_direct_t<FS, PREC, U, 3, true>(a, s) : launch_direct_t<FS, PREC, U, 3, false>(a, s);
+    }
+    constexpr int U = DirectBatch<FS>::U;
+    return epi ? launch_direct_t<FS, PREC, U, 2, true>(a, s) : launch_direct_t<FS, PREC, U, 2, false>(a, s);
 }
 
 }  // namespace
@@ -352,6 +358,14 @@ int sm_count() {
 
 uint32_t window_block_for(uint32_t w_cfg, uint32_t T, uint32_t K, int precision) {
     return choose_config(w_cfg, T, K, precision).wb;
+}
+
+void launch_shape_for(uint32_t w_cfg, uint32_t T, uint32_t K, int precision, int* fs, int* occ,
+                      uint32_t* wb) {
+    const Config c = choose_config(w_cfg, T, K, precision);
+    *fs = c.fs;
+    *occ = c.kernel == kDirect ? c.occ : 2;
+    *wb = c.wb;
 }
 
 uint32_t slice_width_for(uint32_t w_cfg, uint32_t T, uint32_t K, int precision) {
@@ -381,6 +395,9 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     slice_count = std::min(slice_count, slices - slice_begin);
     SpmmArgs a{rwo, tc_offset, bits, a2b, vals, B, C, W, cols, K, cfg.wb, slice_count,
                (W + cfg.wb - 1) / cfg.wb, cfg.slice_major, slice_begin, epi.bias, epi.act};
+    // only the register-direct kernel has the epilogue; it cuts the matrix
+    // into the same pieces as the other variants
+    if (epi.bias || epi.act) cfg.kernel = kDirect;
     if (cfg.kernel == kPipe) return launch_pipe(a, cfg.fs, precision, cfg.nw, cfg.hints, s);
     if (cfg.kernel == kBulk) return launch_bulk(a, cfg.fs, precision, cfg.nw, cfg.hints, s);
     if (cfg.kernel == kLean) return launch_lean(a, cfg.fs, precision, env_int("ACCSPMM_MINB", 4), s);

@@ -184,38 +184,44 @@ struct BitDecode {
     }
 };
 
-// Stores a finished 8-row block of C (rows row0 + 2tq + p, features f0 + 32h
-// + 4g .. + 3), applying the epilogue: + bias[feature], then the activation.
-// Every element of C is stored exactly once, so the epilogue is applied once.
 template <int FS>
-__device__ __forceinline__ void store_rows(const SpmmArgs& a, uint32_t row0, uint32_t f0, int g,
-                                           int tq, float4 (&out)[2][FS / 32]) {
-    if (a.bias || a.act) {
-#pragma unroll
-        for (int h = 0; h < FS / 32; ++h) {
-            const uint32_t f = f0 + 32 * h + 4 * g;
-            float4 b = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (a.bias && f < a.K) b = *reinterpret_cast<const float4*>(a.bias + f);
-#pragma unroll
-            for (int p = 0; p < 2; ++p) {
-                float4& v = out[p][h];
-                v.x += b.x; v.y += b.y; v.z += b.z; v.w += b.w;
-                if (a.act == ACCSPMM_ACT_RELU) {
-                    v.x = fmaxf(v.x, 0.f); v.y = fmaxf(v.y, 0.f);
-                    v.z = fmaxf(v.z, 0.f); v.w = fmaxf(v.w, 0.f);
-                }
-            }
-        }
-    }
+__device__ __forceinline__ void store_rows(float* __restrict__ C, uint32_t K, uint32_t row0,
+                                           uint32_t f0, int g, int tq,
+                                           const float4 (&out)[2][FS / 32]) {
 #pragma unroll
     for (int p = 0; p < 2; ++p) {
-        float* rowp = a.C + size_t(row0 + 2 * tq + p) * a.K;
+        float* rowp = C + size_t(row0 + 2 * tq + p) * K;
 #pragma unroll
         for (int h = 0; h < FS / 32; ++h) {
             uint32_t f = f0 + 32 * h + 4 * g;
-            if (f < a.K) __stcs(reinterpret_cast<float4*>(rowp + f), out[p][h]);
+            if (f < K) __stcs(reinterpret_cast<float4*>(rowp + f), out[p][h]);
         }
     }
+}
+
+// store_rows with the epilogue applied first: + bias[feature], then the
+// activation.  Every element of C is stored exactly once, so the epilogue is
+// applied once.  A separate function (and a compile-time switch in the
+// callers) so that kernels without an epilogue keep their code unchanged.
+template <int FS>
+__device__ __forceinline__ void store_rows_epilogue(const SpmmArgs& a, uint32_t row0, uint32_t f0,
+                                                    int g, int tq, float4 (&out)[2][FS / 32]) {
+#pragma unroll
+    for (int h = 0; h < FS / 32; ++h) {
+        const uint32_t f = f0 + 32 * h + 4 * g;
+        float4 b = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (a.bias && f < a.K) b = *reinterpret_cast<const float4*>(a.bias + f);
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            float4& v = out[p][h];
+            v.x += b.x; v.y += b.y; v.z += b.z; v.w += b.w;
+            if (a.act == ACCSPMM_ACT_RELU) {
+                v.x = fmaxf(v.x, 0.f); v.y = fmaxf(v.y, 0.f);
+                v.z = fmaxf(v.z, 0.f); v.w = fmaxf(v.w, 0.f);
+            }
+        }
+    }
+    store_rows<FS>(a.C, a.K, row0, f0, g, tq, out);
 }
 
 // CTA geometry: window block, feature slice, and the warp pieces of the
@@ -280,7 +286,9 @@ struct Block {
     __device__ __forceinline__ float* slot(int s) const { return part + size_t(s) * 8 * FS; }
 
     // Store a finished window: straight to C if it lies inside [tb, te),
-    // else into this warp's first (is_first) or last partial slot.
+    // else into this warp's first (is_first) or last partial slot.  EPI:
+    // apply the bias / activation epilogue when storing to C.
+    template <bool EPI = false>
     __device__ __forceinline__ void flush(const SpmmArgs& a, const float (&acc)[Layout<H>::NM][4],
                                           uint32_t wloc, uint32_t tb, uint32_t te,
                                           bool is_first) const {
@@ -291,7 +299,8 @@ struct Block {
 #pragma unroll
             for (int h = 0; h < H; ++h) out[p][h] = Layout<H>::get(acc, p, h);
         if (rb >= tb && re <= te) {
-            store_rows<FS>(a, (w0 + wloc) * kWin, f0, g, tq, out);
+            if constexpr (EPI) store_rows_epilogue<FS>(a, (w0 + wloc) * kWin, f0, g, tq, out);
+            else store_rows<FS>(a.C, a.K, (w0 + wloc) * kWin, f0, g, tq, out);
         } else {
             float* sp = slot(2 * warp + (is_first ? 0 : 1));
 #pragma unroll
@@ -304,6 +313,7 @@ struct Block {
 
     // After a CTA barrier: windows cut by piece boundaries are summed from
     // the slots in warp order, empty windows are written as zeros.
+    template <bool EPI = false>
     __device__ __forceinline__ void finish(const SpmmArgs& a) const {
         auto warp_of = [&](uint32_t t) -> int {
             int i = NW - 1;
@@ -334,7 +344,8 @@ struct Block {
                         }
                 }
             }
-            store_rows<FS>(a, (w0 + wloc) * kWin, f0, g, tq, out);
+            if constexpr (EPI) store_rows_epilogue<FS>(a, (w0 + wloc) * kWin, f0, g, tq, out);
+            else store_rows<FS>(a.C, a.K, (w0 + wloc) * kWin, f0, g, tq, out);
         }
     }
 };

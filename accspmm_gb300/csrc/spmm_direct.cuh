@@ -23,7 +23,7 @@ struct DirectBatch {
     static constexpr int U = FS >= 128 ? 2 : (FS == 64 ? 4 : 8);
 };
 
-template <int FS, int PREC, int U = DirectBatch<FS>::U>
+template <int FS, int PREC, int U = DirectBatch<FS>::U, bool EPI = false>
 __device__ __forceinline__ void direct_item(const SpmmArgs& a, const Block<FS, kDirectNW>& blk) {
     constexpr int H = FS / 32;
     using L = Layout<H>;
@@ -94,7 +94,7 @@ __device__ __forceinline__ void direct_item(const SpmmArgs& a, const Block<FS, k
                 const uint32_t tt = t + u;
                 if (tt >= te) break;
                 if (tt >= next_bound) {
-                    blk.flush(a, acc, wl, tb, te, first_win);
+                    blk.template flush<EPI>(a, acc, wl, tb, te, first_win);
                     first_win = false;
 #pragma unroll
                     for (int m = 0; m < NM; ++m) acc[m][0] = acc[m][1] = acc[m][2] = acc[m][3] = 0.f;
@@ -104,10 +104,10 @@ __device__ __forceinline__ void direct_item(const SpmmArgs& a, const Block<FS, k
                 tile_mma<H, PREC>(acc, r0[u], r1[u], av0[u], av1[u]);
             }
         }
-        blk.flush(a, acc, wl, tb, te, first_win);
+        blk.template flush<EPI>(a, acc, wl, tb, te, first_win);
     }
     __syncthreads();
-    blk.finish(a);
+    blk.template finish<EPI>(a);
 }
 
 

@@ -34,6 +34,12 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
                               uint32_t T, uint32_t cols, const float* B, float* C, uint32_t K,
                               int precision, uint32_t slice_begin, uint32_t slice_count,
                               const Epilogue& epi, cudaStream_t s);
+// Slice width, CTAs per SM (register-direct kernel) and windows per CTA the
+// launch-shape chooser picks.
+void launch_shape_for(uint32_t w_cfg, uint32_t T, uint32_t K, int precision, int* fs, int* occ,
+                      uint32_t* wb);
+int gather_floor_impl(const accspmm_metcf_t* m, const float* B, uint32_t K, int repeats,
+                      float* avg_ms, void* stream);
 // Feature columns per slice the launch-shape chooser picks.
 uint32_t slice_width_for(uint32_t w_cfg, uint32_t T, uint32_t K, int precision);
 // rowWindowOffset of W windows derived from an AdpBME's rowIndices (err: a
@@ -47,6 +53,8 @@ int spmm_bias_act_impl(const accspmm_metcf_t* m, const float* B, float* C, uint3
 int gcn_layer_impl(const accspmm_metcf_t* adj, const float* H, uint32_t k_in, const float* W,
                    uint32_t k_out, const float* bias, int act, float* out, int precision,
                    void* stream);
+int permute_rows_impl(const float* src, float* dst, const uint32_t* idx, uint32_t rows, uint32_t K,
+                      int scatter, void* stream);
 // Per-device memory pool of the library (keeps freed memory for later calls).
 int library_pool(cudaMemPool_t* pool);
 int autotune_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K, int precision,

@@ -394,9 +394,13 @@ def run_ours(args):
     U = gathered_rows(m) if rank == 0 else None
     if U is not None:
         gbytes = abytes - 4 * n * K + 4 * K * U
+        # the floor: a launch with the same shape that only gathers those rows
+        floor_ms = m.gather_floor(B, K, 10, stream)
         roofline["gather_model"] = {"bytes": int(gbytes), "gathered_rows": U,
                                     "achieved": round(gbytes / (kms * 1e-3) / 1e9, 1),
-                                    "frac": round(gbytes / (kms * 1e-3) / 1e9 / peak, 4)}
+                                    "frac": round(gbytes / (kms * 1e-3) / 1e9 / peak, 4),
+                                    "floor_ms": round(floor_ms, 4),
+                                    "frac_of_floor": round(floor_ms / kms, 4)}
 
     # end to end through the C ABI with host buffers: accspmm_spmm_host takes
     # B and C in page-locked host memory; every step copies B in (slice by

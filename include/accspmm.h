@@ -190,6 +190,26 @@ int accspmm_coo_copy(const accspmm_coo_t* src, int32_t dst_space,
 int accspmm_adpbme_copy(const accspmm_adpbme_t* src, int32_t dst_space,
                         accspmm_adpbme_t* dst, void* stream);
 
+/* Locality reordering.  No counterpart in the reference, whose benchmark
+ * matrix was reordered offline.  accspmm_reorder_rcm computes a reverse
+ * Cuthill-McKee numbering of a square host CSR (on the pattern of A + A^T,
+ * pseudo-peripheral start vertex per connected component):
+ * perm[new] = old, `rows` entries.  The bandwidth max |row - col| before and
+ * after is reported if the pointers are non-NULL.  accspmm_csr_permute forms
+ * P A P^T on the host (A'[i, j] = A[perm[i], perm[j]], each row's columns
+ * sorted); the result is library-owned.  With it, A B = P^T (A' (P B)):
+ * accspmm_dense_permute_rows gathers (scatter = 0: dst[i] = src[idx[i]]) or
+ * scatters (scatter = 1: dst[idx[i]] = src[i]) the K-float rows of a device
+ * matrix by a device index array of `rows` entries, which must be a
+ * permutation of 0..rows-1 (entries >= rows are skipped). */
+int accspmm_reorder_rcm(const accspmm_csr_t* csr, uint32_t* perm,
+                        uint64_t* bandwidth_before, uint64_t* bandwidth_after);
+int accspmm_csr_permute(const accspmm_csr_t* csr, const uint32_t* perm,
+                        accspmm_csr_t* out);
+int accspmm_dense_permute_rows(const float* src, float* dst, const uint32_t* idx,
+                               uint32_t rows, uint32_t K, int32_t scatter,
+                               void* stream);
+
 /* Binary METCF / AdpBME files.  No counterpart in the reference, which
  * re-parses the .mtx text and rebuilds METCF on every run
  * (src/mma_tf32.cu:196-222).  A file holds the struct's sizes and arrays, each
@@ -303,6 +323,16 @@ int accspmm_time_spmm(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp,
                       const float* B, float* C, uint32_t c_rows, uint32_t K,
                       int32_t precision, int32_t warmup, int32_t exe,
                       float* avg_ms, void* stream);
+
+/* Measurement: the gather floor of accspmm_spmm_tf32 on this matrix and B --
+ * the average time (one warm-up, then `repeats` launches timed with CUDA
+ * events on `stream`) of a kernel that moves exactly the B rows the SpMM
+ * kernel gathers, with the SpMM's launch shape, lane pattern and batching,
+ * and does nothing else (no sparse values, MMAs or C stores).  The SpMM's
+ * time over this floor is how much its arithmetic and bookkeeping cost on
+ * top of its unavoidable row gathers.  No counterpart in the reference. */
+int accspmm_gather_floor(const accspmm_metcf_t* metcf, const float* B, uint32_t K,
+                         int32_t repeats, float* avg_ms, void* stream);
 
 /* ---- autotuning ----------------------------------------------------------- */
 /* No counterpart in the reference (its launch shape is fixed: warps = K/32 or

@@ -116,3 +116,14 @@ def test_argument_errors():
     assert st == capi.ERROR_INVALID_VALUE
     with pytest.raises(capi.AccSpmmError):
         m.spmm_host(Bh, Ch, 6)
+
+
+def test_gather_floor_is_a_positive_time_below_the_spmm():
+    m, cols = device_matrix("powerlaw40k")
+    K = 128
+    B = torch_dev(np.random.default_rng(3).uniform(-1, 1, (cols, K)).astype(np.float32))
+    floor = m.gather_floor(B, K, 5)
+    assert floor > 0
+    C = empty_dev(m.c_rows, K)
+    t = api.time_spmm(m, None, B, C, m.c_rows, K, capi.PREC_TF32, 2, 5)
+    assert floor < 1.5 * t
