@@ -6,7 +6,7 @@
 // one-matrix launch -- the window-block size comes from the same chooser -- so
 // each item's arithmetic, and therefore each result, is bit-identical to the
 // matrix's own accspmm_spmm_tf32 launch.  Items are numbered largest matrix
-// first; resident CTAs (two per SM) take items from an atomic counter until
+// first; resident CTAs (three per SM) take items from an atomic counter until
 // none are left, so uneven matrices share the GPU without a tail of idle SMs.
 // A plan can be captured into a CUDA graph (counter reset + launch) and
 // replayed.
@@ -39,8 +39,10 @@ __device__ __forceinline__ uint32_t find_desc(const BatchDesc* __restrict__ d, u
     return lo;
 }
 
-template <int FS, int PREC>
-__global__ void __launch_bounds__(kNW * 32, 2)
+// U tiles per gather batch and MINB resident CTAs per SM, as in the
+// one-matrix register-direct kernel's default shape.
+template <int FS, int PREC, int U, int MINB>
+__global__ void __launch_bounds__(kNW * 32, MINB)
 spmm_batch_kernel(const BatchDesc* __restrict__ desc, uint32_t n_desc, uint32_t total_items,
                   uint32_t* __restrict__ counter) {
     extern __shared__ __align__(16) float smem[];
@@ -66,7 +68,7 @@ spmm_batch_kernel(const BatchDesc* __restrict__ desc, uint32_t n_desc, uint32_t 
         if (s_item >= total_items) break;
         Block<FS, kNW> blk;
         blk.init_item(s_args, s_wbk, s_slice, s_rwo, part);
-        direct_item_dispatch<FS, PREC>(s_args, blk);
+        direct_item<FS, PREC, U>(s_args, blk);
         __syncthreads();  // s_args, s_rwo and the slots are reused by the next item
     }
 }
@@ -74,26 +76,28 @@ spmm_batch_kernel(const BatchDesc* __restrict__ desc, uint32_t n_desc, uint32_t 
 template <int FS, int PREC>
 int launch_batch_t(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items,
                    uint32_t max_wb, uint32_t* d_counter, cudaStream_t s) {
+    constexpr int kMinB = 3, kU = (DirectBatch<FS>::U + 1) / 2;
     const size_t smem = size_t(2 * kNW * 8 * FS) * 4 + size_t(max_wb + 1) * 4;
     static unsigned attr_set = 0;
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 32 && !(attr_set & (1u << dev))) {
-        ACC_CUDA(cudaFuncSetAttribute(spmm_batch_kernel<FS, PREC>,
+        ACC_CUDA(cudaFuncSetAttribute(spmm_batch_kernel<FS, PREC, kU, kMinB>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
         attr_set |= 1u << dev;
     }
     if (smem > 100 * 1024) ACC_FAIL(ACCSPMM_ERROR_UNSUPPORTED, "window block too large for a batch");
-    const uint32_t grid = std::min<uint32_t>(total_items, uint32_t(sm_count()) * 2);
+    const uint32_t grid = std::min<uint32_t>(total_items, uint32_t(sm_count()) * kMinB);
     if (grid == 0) return ACCSPMM_SUCCESS;
-    spmm_batch_kernel<FS, PREC><<<grid, kNW * 32, smem, s>>>(d_desc, n_desc, total_items, d_counter);
+    spmm_batch_kernel<FS, PREC, kU, kMinB><<<grid, kNW * 32, smem, s>>>(d_desc, n_desc, total_items, d_counter);
     ACC_LAUNCH_CHECK();
     return ACCSPMM_SUCCESS;
 }
 
 }  // namespace
 
-int batch_fs_for(uint32_t max_k) { return max_k <= 32 ? 32 : max_k <= 64 ? 64 : 128; }
+// slice width: the one-matrix default (32 columns for K <= 32, else 64)
+int batch_fs_for(uint32_t max_k) { return max_k <= 32 ? 32 : 64; }
 
 int launch_batch(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items, uint32_t max_wb,
                  uint32_t* d_counter, int fs, int precision, cudaStream_t s) {
@@ -102,10 +106,8 @@ int launch_batch(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items,
     switch (fs) {
         case 32: return x3 ? launch_batch_t<32, ACCSPMM_PREC_3XTF32>(d_desc, n_desc, total_items, max_wb, d_counter, s)
                            : launch_batch_t<32, ACCSPMM_PREC_TF32>(d_desc, n_desc, total_items, max_wb, d_counter, s);
-        case 64: return x3 ? launch_batch_t<64, ACCSPMM_PREC_3XTF32>(d_desc, n_desc, total_items, max_wb, d_counter, s)
+        default: return x3 ? launch_batch_t<64, ACCSPMM_PREC_3XTF32>(d_desc, n_desc, total_items, max_wb, d_counter, s)
                            : launch_batch_t<64, ACCSPMM_PREC_TF32>(d_desc, n_desc, total_items, max_wb, d_counter, s);
-        default: return x3 ? launch_batch_t<128, ACCSPMM_PREC_3XTF32>(d_desc, n_desc, total_items, max_wb, d_counter, s)
-                           : launch_batch_t<128, ACCSPMM_PREC_TF32>(d_desc, n_desc, total_items, max_wb, d_counter, s);
     }
 }
 

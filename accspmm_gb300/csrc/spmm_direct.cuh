@@ -111,9 +111,4 @@ __device__ __forceinline__ void direct_item(const SpmmArgs& a, const Block<FS, k
 }
 
 
-template <int FS, int PREC>
-__device__ __forceinline__ void direct_item_dispatch(const SpmmArgs& a, const Block<FS, kDirectNW>& blk) {
-    direct_item<FS, PREC>(a, blk);
-}
-
 }  // namespace accspmm

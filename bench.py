@@ -58,6 +58,9 @@ def parse():
                    help="scale: the 1M-row SpMM (headline); batch: many graphs in one "
                         "launch vs one launch each; precision: TF32 vs 3xTF32 vs FP64")
     p.add_argument("--graphs", type=int, default=512)
+    p.add_argument("--rows-hi", type=int, default=0,
+                   help="largest graph rows of the batch / serve workloads (default: the "
+                        "stated 200,000 for batch, 500,000 for serve)")
     p.add_argument("--profile", type=int, default=0, metavar="LAUNCHES",
                    help="only build METCF on the GPU and run LAUNCHES plain SpMM launches "
                         "(no timing): the command profiled by ncu")
@@ -514,7 +517,8 @@ def run_batch(args):
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
     prec = capi.PREC_3XTF32 if args.precision == "3xtf32" else capi.PREC_TF32
-    graphs = batch_workload(args.graphs, args.seed)
+    row_hi = args.rows_hi or 200000
+    graphs = batch_workload(args.graphs, args.seed, 1000, row_hi)
     gen = torch.Generator(device=dev).manual_seed(args.seed)
     items, flops = [], 0.0
     for csr, k in graphs:
@@ -563,9 +567,9 @@ def run_batch(args):
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_graph, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": args.precision, "data": "synthetic",
-        "config": {"workload": f"{args.graphs} power-law graphs, rows log-uniform in [1000, 20000] "
-                               "(one tenth of the stated [1000, 200000] range), mean degree "
-                               "uniform in [4, 64], K in {64, 128}",
+        "config": {"workload": f"{args.graphs} power-law graphs, rows log-uniform in [1000, {row_hi}], "
+                               "mean degree uniform in [4, 64], values uniform[0, 1), "
+                               "K in {64, 128}, B uniform[-1, 1)",
                    "graphs": args.graphs, "rows": rows, "nnz": nnz, "work_items": work,
                    "slice_width": fs},
         "batch": {"graph_replay_ms": round(t_graph, 4), "one_launch_ms": round(t_batch, 4),
@@ -659,9 +663,10 @@ def run_serve(args):
     torch.cuda.set_device(0)
     rng = np.random.default_rng(args.seed)
     n_graphs = 64
+    row_hi = args.rows_hi or 500000
     graphs = []
     for i in range(n_graphs):
-        rows = int(np.exp(rng.uniform(np.log(2000), np.log(50000))))
+        rows = int(np.exp(rng.uniform(np.log(2000), np.log(row_hi))))
         deg = synth.powerlaw_degrees(rows, 2.1, 16.0, min(rows, 4096), rng)
         r = np.repeat(np.arange(rows, dtype=np.int64), deg)
         c = rng.integers(0, rows, size=r.size)
@@ -674,7 +679,9 @@ def run_serve(args):
     ks = [32, 64, 128, 256, 512]
     max_rows = max(g.c_rows for g in graphs)
     Bh = torch.empty((max_rows * 512,), dtype=torch.float32, pin_memory=True).uniform_(-1, 1)
-    n_out = 256
+    # output slots in flight: each holds the largest request's C (up to 1 GB
+    # at 500,000 rows x 512 columns), so their number bounds pinned memory
+    n_out = max(16, min(256, (16 << 30) // (max_rows * 512 * 4)))
     Ch = [torch.empty((max_rows * 512,), dtype=torch.float32, pin_memory=True) for _ in range(n_out)]
     prec = capi.PREC_3XTF32 if args.precision == "3xtf32" else capi.PREC_TF32
 
@@ -739,10 +746,11 @@ def run_serve(args):
         "unit": "req/s", "n_gpus": 1, "steps": None, "warmup": None, "ms_per_step": None,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": args.precision, "data": "synthetic",
-        "config": {"workload": "64 resident power-law graphs, rows log-uniform in [2000, 50000] "
-                               "(one tenth of the stated upper bound), mean degree 16, K uniform "
-                               "in {32, 64, 128, 256, 512}, fresh B copied from pinned host "
-                               "memory per request, HBM budget 150 GB",
+        "config": {"workload": f"64 resident power-law graphs, rows log-uniform in [2000, {row_hi}], "
+                               "mean degree 16, K uniform in {32, 64, 128, 256, 512}, fresh B "
+                               "copied from pinned host memory per request, C copied back, "
+                               "HBM budget 150 GB",
+                   "output_slots": n_out,
                    "graph_rows": int(sum(g.struct.rows for g in graphs)),
                    "graph_nnz": int(sum(g.struct.nnz for g in graphs))},
         "serve": results,
