@@ -48,14 +48,14 @@ __device__ __align__(16) float g_zero_row_direct[128] = {0.f};
 // One-matrix launch of the register-direct kernel: one CTA per work item.
 // U tiles per batch; MINB resident CTAs per SM (the register budget); EPI:
 // the bias / activation epilogue is applied as C is stored.
-template <int FS, int PREC, int U, int MINB, bool EPI>
-__global__ void __launch_bounds__(kNW * 32, MINB) spmm_window_kernel(const SpmmArgs a) {
+template <int FS, int PREC, int U, int MINB, bool EPI, int NW = kNW>
+__global__ void __launch_bounds__(NW * 32, MINB) spmm_window_kernel(const SpmmArgs a) {
     extern __shared__ __align__(16) float smem[];
-    float* part = smem;  // [2 * kNW] slots
-    uint32_t* s_rwo = reinterpret_cast<uint32_t*>(smem + 2 * kNW * 8 * FS);
-    Block<FS, kNW> blk;
+    float* part = smem;  // [2 * NW] slots
+    uint32_t* s_rwo = reinterpret_cast<uint32_t*>(smem + 2 * NW * 8 * FS);
+    Block<FS, NW> blk;
     blk.init(a, s_rwo, part);
-    direct_item<FS, PREC, U, EPI>(a, blk);
+    direct_item<FS, PREC, U, EPI, NW>(a, blk);
 }
 
 // Double-buffered register-direct kernel: the gathers of batch q + 1 are
@@ -296,7 +296,7 @@ Config choose_config(uint32_t W, uint32_t T, uint32_t K, int precision) {
     int fs = env_int("ACCSPMM_FS", 0);
     if (fs == 32 || fs == 64 || fs == 128) c.fs = fs;
     int occ = env_int("ACCSPMM_OCC", 0);
-    if (occ == 2 || occ == 3) c.occ = occ;
+    if (occ >= 2 && occ <= 5) c.occ = occ;
     int nw = env_int("ACCSPMM_NW", 0);
     if (nw == 2 || nw == 4 || nw == 8) c.nw = nw;
     if (c.kernel == kPipe && c.fs >= 64) c.nw = 4;  // stage ring must fit in shared memory
@@ -308,21 +308,21 @@ Config choose_config(uint32_t W, uint32_t T, uint32_t K, int precision) {
     return c;
 }
 
-template <int FS, int PREC, int U, int MINB, bool EPI>
+template <int FS, int PREC, int U, int MINB, bool EPI, int NW = kNW>
 int launch_direct_t(const SpmmArgs& a, cudaStream_t s) {
-    const size_t smem = size_t(2 * kNW * 8 * FS) * 4 + size_t(a.wb + 1) * 4;
+    const size_t smem = size_t(2 * NW * 8 * FS) * 4 + size_t(a.wb + 1) * 4;
     static unsigned attr_set = 0;  // one bit per device
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 32 && !(attr_set & (1u << dev))) {
-        ACC_CUDA(cudaFuncSetAttribute(spmm_window_kernel<FS, PREC, U, MINB, EPI>,
+        ACC_CUDA(cudaFuncSetAttribute(spmm_window_kernel<FS, PREC, U, MINB, EPI, NW>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
         attr_set |= 1u << dev;
     }
     const uint64_t grid = uint64_t(a.n_wblocks) * a.n_slices;
     if (grid == 0) return ACCSPMM_SUCCESS;
     if (grid > 0x7FFFFFFFull) ACC_FAIL(ACCSPMM_ERROR_OVERFLOW, "grid too large");
-    spmm_window_kernel<FS, PREC, U, MINB, EPI><<<unsigned(grid), kNW * 32, smem, s>>>(a);
+    spmm_window_kernel<FS, PREC, U, MINB, EPI, NW><<<unsigned(grid), NW * 32, smem, s>>>(a);
     ACC_LAUNCH_CHECK();
     return ACCSPMM_SUCCESS;
 }
@@ -336,6 +336,11 @@ int launch_direct(const SpmmArgs& a, int occ, cudaStream_t s) {
     if (occ == 3) {
         constexpr int U = (DirectBatch<FS>::U + 1) / 2;
         return epi ? launch_direct_t<FS, PREC, U, 3, true>(a, s) : launch_direct_t<FS, PREC, U, 3, false>(a, s);
+    }
+    if constexpr (FS == 128) {
+        // 4 warps per CTA: 128-column slices at 96 or 128 registers a thread
+        if (occ == 5 && !epi) return launch_direct_t<FS, PREC, 1, 5, false, 4>(a, s);
+        if (occ == 4 && !epi) return launch_direct_t<FS, PREC, 2, 4, false, 4>(a, s);
     }
     constexpr int U = DirectBatch<FS>::U;
     return epi ? launch_direct_t<FS, PREC, U, 2, true>(a, s) : launch_direct_t<FS, PREC, U, 2, false>(a, s);

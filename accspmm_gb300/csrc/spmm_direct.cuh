@@ -23,8 +23,8 @@ struct DirectBatch {
     static constexpr int U = FS >= 128 ? 2 : (FS == 64 ? 4 : 8);
 };
 
-template <int FS, int PREC, int U = DirectBatch<FS>::U, bool EPI = false>
-__device__ __forceinline__ void direct_item(const SpmmArgs& a, const Block<FS, kDirectNW>& blk) {
+template <int FS, int PREC, int U = DirectBatch<FS>::U, bool EPI = false, int NW = kDirectNW>
+__device__ __forceinline__ void direct_item(const SpmmArgs& a, const Block<FS, NW>& blk) {
     constexpr int H = FS / 32;
     using L = Layout<H>;
     constexpr int NM = L::NM;

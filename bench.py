@@ -679,32 +679,62 @@ def run_serve(args):
     ks = [32, 64, 128, 256, 512]
     max_rows = max(g.c_rows for g in graphs)
     Bh = torch.empty((max_rows * 512,), dtype=torch.float32, pin_memory=True).uniform_(-1, 1)
-    # output slots in flight: each holds the largest request's C (up to 1 GB
-    # at 500,000 rows x 512 columns), so their number bounds pinned memory
-    n_out = max(16, min(256, (16 << 30) // (max_rows * 512 * 4)))
-    Ch = [torch.empty((max_rows * 512,), dtype=torch.float32, pin_memory=True) for _ in range(n_out)]
+    # outputs: one page-locked arena from which each request takes exactly its
+    # C (c_rows x K floats) and returns it when done, so the number of
+    # requests in flight is bounded by bytes, not by worst-case slots
+    arena_floats = (24 << 30) // 4
+    arena = torch.empty((arena_floats,), dtype=torch.float32, pin_memory=True)
     prec = capi.PREC_3XTF32 if args.precision == "3xtf32" else capi.PREC_TF32
+
+    class Arena:
+        """First-fit allocator over the arena (offsets in floats, 64-float
+        granules), with a condition variable for callers waiting on space."""
+
+        def __init__(self, n):
+            self.free = [(0, n)]
+            self.cv = threading.Condition()
+
+        def get(self, size):
+            size = (size + 63) // 64 * 64
+            with self.cv:
+                while True:
+                    for idx, (off, n) in enumerate(self.free):
+                        if n >= size:
+                            if n == size:
+                                self.free.pop(idx)
+                            else:
+                                self.free[idx] = (off + size, n - size)
+                            return off, size
+                    self.cv.wait()
+
+        def put(self, off, size):
+            with self.cv:
+                self.free.append((off, size))
+                self.free.sort()
+                merged = []
+                for o, n in self.free:
+                    if merged and merged[-1][0] + merged[-1][1] == o:
+                        merged[-1] = (merged[-1][0], merged[-1][1] + n)
+                    else:
+                        merged.append((o, n))
+                self.free = merged
+                self.cv.notify_all()
 
     def drive(srv, rate, n_req):
         arr = np.cumsum(rng.exponential(1.0 / rate, size=n_req))
         g_of = rng.integers(0, n_graphs, size=n_req)
         k_of = rng.choice(ks, size=n_req)
         ids = [None] * n_req
-        free = threading.Semaphore(n_out)
-        slots = list(range(n_out))
-        lock = threading.Lock()
-        done_slots = []
+        pool = Arena(arena_floats)
 
         def waiter():
             for i in range(n_req):
                 while ids[i] is None:
                     time.sleep(0.0001)
-                rid, slot = ids[i]
+                rid, off, size = ids[i]
                 st = srv.wait(rid, 120000)
                 assert st == 0, st
-                with lock:
-                    slots.append(slot)
-                free.release()
+                pool.put(off, size)
 
         th = threading.Thread(target=waiter)
         th.start()
@@ -713,12 +743,10 @@ def run_serve(args):
             wait_s = t0 + arr[i] - time.perf_counter()
             if wait_s > 0:
                 time.sleep(wait_s)
-            free.acquire()
-            with lock:
-                slot = slots.pop()
             g, k = int(g_of[i]), int(k_of[i])
-            rid = srv.submit(g, Bh, Ch[slot], k, prec)
-            ids[i] = (rid, slot)
+            off, size = pool.get(graphs[g].c_rows * k)
+            rid = srv.submit(g, Bh, arena[off:off + size], k, prec)
+            ids[i] = (rid, off, size)
         th.join()
         return srv.stats()
 
@@ -750,7 +778,7 @@ def run_serve(args):
                                "mean degree 16, K uniform in {32, 64, 128, 256, 512}, fresh B "
                                "copied from pinned host memory per request, C copied back, "
                                "HBM budget 150 GB",
-                   "output_slots": n_out,
+                   "output_arena_gb": arena_floats * 4 / (1 << 30),
                    "graph_rows": int(sum(g.struct.rows for g in graphs)),
                    "graph_nnz": int(sum(g.struct.nnz for g in graphs))},
         "serve": results,
