@@ -61,8 +61,8 @@ __global__ void __launch_bounds__(NW * 32, MINB) spmm_window_kernel(const SpmmAr
 // Double-buffered register-direct kernel: the gathers of batch q + 1 are
 // issued before the MMAs of batch q, so every warp keeps a batch of B rows
 // in flight while it computes instead of alternating load and compute phases.
-template <int FS, int PREC, int U>
-__global__ void __launch_bounds__(kNW * 32, 2) spmm_db_kernel(const SpmmArgs a) {
+template <int FS, int PREC, int U, int MINB = 2>
+__global__ void __launch_bounds__(kNW * 32, MINB) spmm_db_kernel(const SpmmArgs a) {
     constexpr int H = FS / 32;
     using L = Layout<H>;
     constexpr int NM = L::NM;
@@ -176,21 +176,21 @@ __global__ void __launch_bounds__(kNW * 32, 2) spmm_db_kernel(const SpmmArgs a) 
     blk.finish(a);
 }
 
-template <int FS, int PREC, int U>
+template <int FS, int PREC, int U, int MINB = 2>
 int launch_db(const SpmmArgs& a, cudaStream_t s) {
     const size_t smem = size_t(2 * kNW * 8 * FS) * 4 + size_t(a.wb + 1) * 4;
     static unsigned attr_set = 0;  // one bit per device
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 32 && !(attr_set & (1u << dev))) {
-        ACC_CUDA(cudaFuncSetAttribute(spmm_db_kernel<FS, PREC, U>,
+        ACC_CUDA(cudaFuncSetAttribute(spmm_db_kernel<FS, PREC, U, MINB>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
         attr_set |= 1u << dev;
     }
     const uint64_t grid = uint64_t(a.n_wblocks) * a.n_slices;
     if (grid == 0) return ACCSPMM_SUCCESS;
     if (grid > 0x7FFFFFFFull) ACC_FAIL(ACCSPMM_ERROR_OVERFLOW, "grid too large");
-    spmm_db_kernel<FS, PREC, U><<<unsigned(grid), kNW * 32, smem, s>>>(a);
+    spmm_db_kernel<FS, PREC, U, MINB><<<unsigned(grid), kNW * 32, smem, s>>>(a);
     ACC_LAUNCH_CHECK();
     return ACCSPMM_SUCCESS;
 }
@@ -296,7 +296,7 @@ Config choose_config(uint32_t W, uint32_t T, uint32_t K, int precision) {
     int fs = env_int("ACCSPMM_FS", 0);
     if (fs == 32 || fs == 64 || fs == 128) c.fs = fs;
     int occ = env_int("ACCSPMM_OCC", 0);
-    if (occ >= 2 && occ <= 5) c.occ = occ;
+    if (occ == 2 || occ == 3) c.occ = occ;
     int nw = env_int("ACCSPMM_NW", 0);
     if (nw == 2 || nw == 4 || nw == 8) c.nw = nw;
     if (c.kernel == kPipe && c.fs >= 64) c.nw = 4;  // stage ring must fit in shared memory
@@ -336,11 +336,6 @@ int launch_direct(const SpmmArgs& a, int occ, cudaStream_t s) {
     if (occ == 3) {
         constexpr int U = (DirectBatch<FS>::U + 1) / 2;
         return epi ? launch_direct_t<FS, PREC, U, 3, true>(a, s) : launch_direct_t<FS, PREC, U, 3, false>(a, s);
-    }
-    if constexpr (FS == 128) {
-        // 4 warps per CTA: 128-column slices at 96 or 128 registers a thread
-        if (occ == 5 && !epi) return launch_direct_t<FS, PREC, 1, 5, false, 4>(a, s);
-        if (occ == 4 && !epi) return launch_direct_t<FS, PREC, 2, 4, false, 4>(a, s);
     }
     constexpr int U = DirectBatch<FS>::U;
     return epi ? launch_direct_t<FS, PREC, U, 2, true>(a, s) : launch_direct_t<FS, PREC, U, 2, false>(a, s);
