@@ -176,6 +176,20 @@ def measured_traffic(K):
     return None
 
 
+def replica_throughput(ms: float, flops_per_step: float, world: int, device=None):
+    """Whole-job figures of N independent replicas: the step time is the
+    slowest rank's (max over ranks, one all-reduce when world > 1) and the
+    throughput counts every rank's work.  Returns (ms, GFLOP/s)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    return ms, flops_per_step * world / (ms * 1e-3) / 1e9
+
+
 def cusparse_comparator(rp, ci, v, B, reps=10):
     """cuSPARSE CSR SpMM (through torch.sparse, FP32 arithmetic) on the same
     matrix and B: the vendor library's time for the same product, reported
@@ -363,13 +377,8 @@ def run_ours(args):
         e1.record(stream)
         torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
     flops = 2.0 * nnz * K
-    value = flops * world / (ms * 1e-3) / 1e9
+    ms, value = replica_throughput(ms, flops, world, dev)
 
     # dominant kernel alone: the plain entry point is exactly one launch of it
     for _ in range(3):
