@@ -339,6 +339,12 @@ class DeviceMETCF(DeviceObject):
         call("accspmm_spmm_bias_act", self.ref, C.c_void_p(_addr(B)), C.c_void_p(_addr(C_out)), K,
              precision, C.c_void_p(_addr(bias)), activation, _stream(stream))
 
+    def spmm_chain(self, B, C_out, K: int, hops: int = 2, precision: int = capi.PREC_TF32,
+                   stream=None) -> None:
+        """C_out = A^hops * B on the device (accspmm_spmm_chain)."""
+        call("accspmm_spmm_chain", self.ref, C.c_void_p(_addr(B)), C.c_void_p(_addr(C_out)), K,
+             hops, precision, _stream(stream))
+
     def gather_floor(self, B, K: int, repeats: int = 10, stream=None) -> float:
         """Milliseconds of a launch that only gathers the B rows this SpMM
         reads (accspmm_gather_floor)."""

@@ -372,6 +372,12 @@ int accspmm_gcn_layer(const accspmm_metcf_t* adj, const float* H, uint32_t k_in,
     return gcn_layer_impl(adj, H, k_in, W, k_out, bias, activation, out, precision, stream);
 }
 
+int accspmm_spmm_chain(const accspmm_metcf_t* metcf, const float* B, float* C, uint32_t K,
+                       uint32_t hops, int32_t precision, void* stream) {
+    clear_error();
+    return spmm_chain_impl(metcf, B, C, K, hops, precision, stream);
+}
+
 int accspmm_gather_floor(const accspmm_metcf_t* metcf, const float* B, uint32_t K,
                          int32_t repeats, float* avg_ms, void* stream) {
     clear_error();

@@ -55,6 +55,8 @@ int gcn_layer_impl(const accspmm_metcf_t* adj, const float* H, uint32_t k_in, co
                    void* stream);
 int permute_rows_impl(const float* src, float* dst, const uint32_t* idx, uint32_t rows, uint32_t K,
                       int scatter, void* stream);
+int spmm_chain_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K, uint32_t hops,
+                    int precision, void* stream);
 // Per-device memory pool of the library (keeps freed memory for later calls).
 int library_pool(cudaMemPool_t* pool);
 int autotune_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K, int precision,

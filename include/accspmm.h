@@ -273,6 +273,14 @@ int accspmm_gcn_layer(const accspmm_metcf_t* adj, const float* H, uint32_t k_in,
                       int32_t activation, float* out, int32_t precision,
                       void* stream);
 
+/* Multi-hop propagation C = A^hops B of a square matrix, all on the device:
+ * hops launches of accspmm_spmm_tf32, each product feeding the next through
+ * intermediates (8 num_windows x K) from the library's memory pool, no host
+ * round trip.  The two-hop case is the A (A B) chain of the request server.
+ * No counterpart in the reference. */
+int accspmm_spmm_chain(const accspmm_metcf_t* metcf, const float* B, float* C,
+                       uint32_t K, uint32_t hops, int32_t precision, void* stream);
+
 /* SpMM with B and C in host memory: the host wrappers tf32_spmm and
  * adp_tf32_spmm, src/mma_tf32.cu:12-183 (device buffers, B copied in, one
  * kernel, C copied out), as one pipelined call.  Pass exactly one of `metcf`

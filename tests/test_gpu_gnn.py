@@ -76,3 +76,26 @@ def test_epilogue_argument_errors():
     assert e.value.status == capi.ERROR_INVALID_VALUE
     with pytest.raises(capi.AccSpmmError):
         m.spmm_bias_act(B, C, 8, None, 7)
+
+
+@pytest.mark.parametrize("hops", [1, 2, 3, 4])
+def test_chain_equals_repeated_spmm(hops):
+    m, csr = device_matrix("plsym1000")
+    K = 64
+    B = torch_dev(np.random.default_rng(hops).uniform(-1, 1, (csr["cols"], K)).astype(np.float32))
+    want = B
+    for _ in range(hops):
+        nxt = empty_dev(m.c_rows, K)
+        m.spmm(want, nxt, K)
+        want = nxt
+    got = empty_dev(m.c_rows, K)
+    m.spmm_chain(B, got, K, hops)
+    torch.cuda.synchronize()
+    assert torch.equal(got, want)
+
+
+def test_chain_needs_a_square_matrix():
+    m, csr = device_matrix("longwin")  # 64 x 600
+    B = empty_dev(csr["cols"], 8, 0.0)
+    with pytest.raises(capi.AccSpmmError):
+        m.spmm_chain(B, empty_dev(m.c_rows, 8), 8, 2)
