@@ -11,6 +11,7 @@
 // A plan can be captured into a CUDA graph (counter reset + launch) and
 // replayed.
 #include <algorithm>
+#include <cstdlib>
 #include <numeric>
 #include <vector>
 
@@ -41,7 +42,7 @@ __device__ __forceinline__ uint32_t find_desc(const BatchDesc* __restrict__ d, u
 
 // U tiles per gather batch and MINB resident CTAs per SM, as in the
 // one-matrix register-direct kernel's default shape.
-template <int FS, int PREC, int U, int MINB>
+template <int FS, int PREC, int U, int MINB, bool ROLL>
 __global__ void __launch_bounds__(kNW * 32, MINB)
 spmm_batch_kernel(const BatchDesc* __restrict__ desc, uint32_t n_desc, uint32_t total_items,
                   uint32_t* __restrict__ counter) {
@@ -68,12 +69,12 @@ spmm_batch_kernel(const BatchDesc* __restrict__ desc, uint32_t n_desc, uint32_t 
         if (s_item >= total_items) break;
         Block<FS, kNW> blk;
         blk.init_item(s_args, s_wbk, s_slice, s_rwo, part);
-        direct_item<FS, PREC, U>(s_args, blk);
+        direct_item<FS, PREC, U, false, kNW, ROLL>(s_args, blk);
         __syncthreads();  // s_args, s_rwo and the slots are reused by the next item
     }
 }
 
-template <int FS, int PREC>
+template <int FS, int PREC, bool ROLL>
 int launch_batch_t(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items,
                    uint32_t max_wb, uint32_t* d_counter, cudaStream_t s) {
     constexpr int kMinB = 3, kU = (DirectBatch<FS>::U + 1) / 2;
@@ -82,14 +83,14 @@ int launch_batch_t(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_item
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 32 && !(attr_set & (1u << dev))) {
-        ACC_CUDA(cudaFuncSetAttribute(spmm_batch_kernel<FS, PREC, kU, kMinB>,
+        ACC_CUDA(cudaFuncSetAttribute(spmm_batch_kernel<FS, PREC, kU, kMinB, ROLL>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
         attr_set |= 1u << dev;
     }
     if (smem > 100 * 1024) ACC_FAIL(ACCSPMM_ERROR_UNSUPPORTED, "window block too large for a batch");
     const uint32_t grid = std::min<uint32_t>(total_items, uint32_t(sm_count()) * kMinB);
     if (grid == 0) return ACCSPMM_SUCCESS;
-    spmm_batch_kernel<FS, PREC, kU, kMinB><<<grid, kNW * 32, smem, s>>>(d_desc, n_desc, total_items, d_counter);
+    spmm_batch_kernel<FS, PREC, kU, kMinB, ROLL><<<grid, kNW * 32, smem, s>>>(d_desc, n_desc, total_items, d_counter);
     ACC_LAUNCH_CHECK();
     return ACCSPMM_SUCCESS;
 }
@@ -103,11 +104,19 @@ int launch_batch(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items,
                  uint32_t* d_counter, int fs, int precision, cudaStream_t s) {
     ACC_CUDA(cudaMemsetAsync(d_counter, 0, 4, s));
     const bool x3 = precision == ACCSPMM_PREC_3XTF32;
+    // the rolling tile ring spills in the persistent kernel (24 bytes) and
+    // measured 6 % slower on 128 power-law graphs: off unless ACCSPMM_ROLL=1
+    const char* e = std::getenv("ACCSPMM_ROLL");
+    const bool roll = e && *e == '1';
     switch (fs) {
-        case 32: return x3 ? launch_batch_t<32, ACCSPMM_PREC_3XTF32>(d_desc, n_desc, total_items, max_wb, d_counter, s)
-                           : launch_batch_t<32, ACCSPMM_PREC_TF32>(d_desc, n_desc, total_items, max_wb, d_counter, s);
-        default: return x3 ? launch_batch_t<64, ACCSPMM_PREC_3XTF32>(d_desc, n_desc, total_items, max_wb, d_counter, s)
-                           : launch_batch_t<64, ACCSPMM_PREC_TF32>(d_desc, n_desc, total_items, max_wb, d_counter, s);
+        case 32: return x3 ? launch_batch_t<32, ACCSPMM_PREC_3XTF32, false>(d_desc, n_desc, total_items, max_wb, d_counter, s)
+                           : launch_batch_t<32, ACCSPMM_PREC_TF32, false>(d_desc, n_desc, total_items, max_wb, d_counter, s);
+        default:
+            if (roll)
+                return x3 ? launch_batch_t<64, ACCSPMM_PREC_3XTF32, true>(d_desc, n_desc, total_items, max_wb, d_counter, s)
+                          : launch_batch_t<64, ACCSPMM_PREC_TF32, true>(d_desc, n_desc, total_items, max_wb, d_counter, s);
+            return x3 ? launch_batch_t<64, ACCSPMM_PREC_3XTF32, false>(d_desc, n_desc, total_items, max_wb, d_counter, s)
+                      : launch_batch_t<64, ACCSPMM_PREC_TF32, false>(d_desc, n_desc, total_items, max_wb, d_counter, s);
     }
 }
 

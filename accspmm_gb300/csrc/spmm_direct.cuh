@@ -23,7 +23,11 @@ struct DirectBatch {
     static constexpr int U = FS >= 128 ? 2 : (FS == 64 ? 4 : 8);
 };
 
-template <int FS, int PREC, int U = DirectBatch<FS>::U, bool EPI = false, int NW = kDirectNW>
+// ROLL: a register ring of U tile slots, each reloaded with the tile U ahead
+// as soon as its MMAs have consumed it, instead of a whole batch of loads
+// followed by a whole batch of MMAs.
+template <int FS, int PREC, int U = DirectBatch<FS>::U, bool EPI = false, int NW = kDirectNW,
+          bool ROLL = false>
 __device__ __forceinline__ void direct_item(const SpmmArgs& a, const Block<FS, NW>& blk) {
     constexpr int H = FS / 32;
     using L = Layout<H>;
@@ -65,6 +69,54 @@ __device__ __forceinline__ void direct_item(const SpmmArgs& a, const Block<FS, N
         BitDecode dec;
         dec.init(g, tq);
         const float* Bl = a.B + blk.f0 + 4 * g;
+        if constexpr (ROLL) {
+            float av0[U], av1[U];
+            float4 r0[U][H], r1[U][H];
+            // loads tile (batch of ma/mb/mo) + u into slot u; tiles past te
+            // carry padding metadata and load nothing
+            auto issue = [&](int u) {
+                const uint32_t i0 = __shfl_sync(0xffffffffu, ma[(8 * u) / 32], (8 * u + tq) & 31);
+                const uint32_t i1 = __shfl_sync(0xffffffffu, ma[(8 * u) / 32], (8 * u + tq + 4) & 31);
+                const uint64_t bm = shfl_u64(mb, u);
+                const uint32_t to = __shfl_sync(0xffffffffu, mo, u);
+                uint32_t x0, x1;
+                bool q0, q1;
+                dec.decode(bm, x0, x1, q0, q1);
+                av0[u] = q0 ? ldg_f32_ordered(a.vals + to + x0) : 0.f;
+                av1[u] = q1 ? ldg_f32_ordered(a.vals + to + x1) : 0.f;
+                const bool v0 = i0 < a.cols, v1 = i1 < a.cols;
+                const float* p0 = Bl + size_t(v0 ? i0 : 0) * a.K;
+                const float* p1 = Bl + size_t(v1 ? i1 : 0) * a.K;
+#pragma unroll
+                for (int h = 0; h < H; ++h) {
+                    r0[u][h] = (v0 && fok[h]) ? ldg_f4_ordered(p0 + 32 * h) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    r1[u][h] = (v1 && fok[h]) ? ldg_f4_ordered(p1 + 32 * h) : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+            };
+#pragma unroll
+            for (int u = 0; u < U; ++u) issue(u);
+            load_meta(tb + U);  // padding when past te
+            for (uint32_t t = tb; t < te; t += U) {
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const uint32_t tt = t + u;
+                    if (tt < te) {
+                        if (tt >= next_bound) {
+                            blk.template flush<EPI>(a, acc, wl, tb, te, first_win);
+                            first_win = false;
+#pragma unroll
+                            for (int m = 0; m < NM; ++m) acc[m][0] = acc[m][1] = acc[m][2] = acc[m][3] = 0.f;
+                            while (blk.s_rwo[wl + 1] <= tt) ++wl;
+                            next_bound = blk.s_rwo[wl + 1];
+                        }
+                        tile_mma<H, PREC>(acc, r0[u], r1[u], av0[u], av1[u]);
+                    }
+                    issue(u);  // tile t + U + u
+                }
+                load_meta(t + 2 * U);
+            }
+            blk.template flush<EPI>(a, acc, wl, tb, te, first_win);
+        } else {
         for (uint32_t t = tb; t < te; t += U) {
             float av0[U], av1[U];
             float4 r0[U][H], r1[U][H];
@@ -105,6 +157,7 @@ __device__ __forceinline__ void direct_item(const SpmmArgs& a, const Block<FS, N
             }
         }
         blk.template flush<EPI>(a, acc, wl, tb, te, first_win);
+        }
     }
     __syncthreads();
     blk.template finish<EPI>(a);
