@@ -351,6 +351,7 @@ int launch_direct(const SpmmArgs& a, int occ, cudaStream_t s) {
         return launch_direct_t<FS, PREC, U, 3, false>(a, s);
     }
     constexpr int U = DirectBatch<FS>::U;
+    if (!epi && env_int("ACCSPMM_ROLL", -1) == 1) return launch_direct_t<FS, PREC, U, 2, false, kNW, true>(a, s);
     return epi ? launch_direct_t<FS, PREC, U, 2, true>(a, s) : launch_direct_t<FS, PREC, U, 2, false>(a, s);
 }
 
