@@ -345,12 +345,13 @@ class DeviceMETCF(DeviceObject):
         call("accspmm_spmm_chain", self.ref, C.c_void_p(_addr(B)), C.c_void_p(_addr(C_out)), K,
              hops, precision, _stream(stream))
 
-    def gather_floor(self, B, K: int, repeats: int = 10, stream=None) -> float:
+    def gather_floor(self, B, K: int, repeats: int = 10, stream=None, slice_width: int = 0) -> float:
         """Milliseconds of a launch that only gathers the B rows this SpMM
-        reads (accspmm_gather_floor)."""
+        reads (accspmm_gather_floor), in the SpMM's launch shape or in the
+        register-direct shape of another slice width."""
         ms = C.c_float(0.0)
-        call("accspmm_gather_floor", self.ref, C.c_void_p(_addr(B)), K, repeats, C.byref(ms),
-             _stream(stream))
+        call("accspmm_gather_floor", self.ref, C.c_void_p(_addr(B)), K, slice_width, repeats,
+             C.byref(ms), _stream(stream))
         return float(ms.value)
 
     def gcn_layer(self, H, k_in: int, W, k_out: int, out, bias=None,

@@ -137,7 +137,7 @@ _SIGS = {
     "accspmm_spmm_bias_act": ([C.POINTER(METCF), vp, vp, u32, i32, vp, i32, vp], C.c_int),
     "accspmm_gcn_layer": ([C.POINTER(METCF), vp, u32, vp, u32, vp, i32, vp, i32, vp], C.c_int),
     "accspmm_spmm_chain": ([C.POINTER(METCF), vp, vp, u32, u32, i32, vp], C.c_int),
-    "accspmm_gather_floor": ([C.POINTER(METCF), vp, u32, i32, f32p, vp], C.c_int),
+    "accspmm_gather_floor": ([C.POINTER(METCF), vp, u32, u32, i32, f32p, vp], C.c_int),
     "accspmm_spmm_host": ([C.POINTER(METCF), C.POINTER(ADPBME), vp, vp, u32, i32, vp], C.c_int),
     "accspmm_spmm_adaptive_noalloc": ([C.POINTER(ADPBME), vp, vp, u32, u32, i32, vp], C.c_int),
     "accspmm_noalloc_max_c_rows": ([], C.c_uint32),

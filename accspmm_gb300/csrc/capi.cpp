@@ -379,9 +379,9 @@ int accspmm_spmm_chain(const accspmm_metcf_t* metcf, const float* B, float* C, u
 }
 
 int accspmm_gather_floor(const accspmm_metcf_t* metcf, const float* B, uint32_t K,
-                         int32_t repeats, float* avg_ms, void* stream) {
+                         uint32_t slice_width, int32_t repeats, float* avg_ms, void* stream) {
     clear_error();
-    return gather_floor_impl(metcf, B, K, repeats, avg_ms, stream);
+    return gather_floor_impl(metcf, B, K, slice_width, repeats, avg_ms, stream);
 }
 
 int accspmm_spmm_host(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp,

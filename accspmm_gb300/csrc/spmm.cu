@@ -260,19 +260,23 @@ std::map<TuneKey, Config> g_tuned;
 thread_local const Config* g_forced = nullptr;
 
 // Launch shape from (W, T, K, precision).  Defaults measured on GB300 with
-// the 1M-row power-law workload (K = 32 ... 256): the register-direct kernel
-// at 3 CTAs per SM (24 warps, a smaller gather batch per warp) with 64-column
-// slices (32 for K <= 32) and 32 windows per CTA, fewer for small matrices so
-// that every SM gets work; 10-20 % faster than 2 CTAs per SM with 128-column
-// slices.  A shape found by accspmm_autotune_metcf for the same signature
-// replaces the default; environment variables override both for experiments
-// (ACCSPMM_KERNEL, _FS, _OCC, _WB, _NW, _ORDER, _HINTS).
+// the 1M-row power-law workload (K = 32 ... 256), all register-direct with up
+// to 32 windows per CTA (fewer for small matrices so that every SM gets work):
+//  - TF32, K > 64: 128-column slices at 2 CTAs per SM with the rolling
+//    two-tile ring (one slice decodes each tile once);
+//  - TF32, 32 < K <= 64: 64-column slices at 3 CTAs per SM with the ring;
+//  - 3xTF32 (K > 32): 64-column slices at 3 CTAs per SM, batch then compute
+//    (the ring spills there);
+//  - K <= 32: 32-column slices at 3 CTAs per SM, batch then compute.
+// A shape found by accspmm_autotune_metcf for the same signature replaces
+// the default; environment variables override both for experiments
+// (ACCSPMM_KERNEL, _FS, _OCC, _ROLL, _WB, _NW, _ORDER, _HINTS).
 Config choose_config(uint32_t W, uint32_t T, uint32_t K, int precision) {
     if (g_forced) return *g_forced;
     Config c;
     c.kernel = kDirect;
-    c.fs = K <= 32 ? 32 : 64;
-    c.occ = 3;
+    c.fs = K <= 32 ? 32 : (K <= 64 || precision == ACCSPMM_PREC_3XTF32) ? 64 : 128;
+    c.occ = c.fs == 128 ? 2 : 3;
     c.nw = c.fs == 32 ? 8 : 4;
     c.hints = 1;
     c.slice_major = 0;
@@ -327,11 +331,12 @@ int launch_direct_t(const SpmmArgs& a, cudaStream_t s) {
     return ACCSPMM_SUCCESS;
 }
 
-// Whether the register-direct kernel at 3 CTAs per SM uses the rolling tile
-// ring by default (measured on GB300, 1M-row workload: 8-9 % faster for TF32
-// at 64 columns; slower where the ring spills: 32 columns, 3xTF32).
-template <int FS, int PREC>
-constexpr bool kRollDefault = FS == 64 && PREC == ACCSPMM_PREC_TF32;
+// Whether the register-direct kernel uses the rolling tile ring by default
+// (measured on GB300, 1M-row workload: 8-9 % faster for TF32 at 64 columns
+// and 3 CTAs per SM, 3-4 % faster again at 128 columns and 2 CTAs per SM;
+// slower where the ring spills: 32 columns, 3xTF32).
+template <int FS, int PREC, int MINB>
+constexpr bool kRollDefault = PREC == ACCSPMM_PREC_TF32 && ((FS == 64 && MINB == 3) || (FS == 128 && MINB == 2));
 
 // occ = 2: the batch of DirectBatch (64 floats of B per lane in flight) at 2
 // CTAs per SM; occ = 3: half that batch at 3 CTAs per SM (80 registers a
@@ -342,7 +347,7 @@ int launch_direct(const SpmmArgs& a, int occ, cudaStream_t s) {
     if (occ == 3) {
         constexpr int U = (DirectBatch<FS>::U + 1) / 2;
         const int roll = env_int("ACCSPMM_ROLL", -1);
-        const bool use_roll = roll < 0 ? kRollDefault<FS, PREC> : roll != 0;
+        const bool use_roll = roll < 0 ? kRollDefault<FS, PREC, 3> : roll != 0;
         if (use_roll) {
             if (epi) return launch_direct_t<FS, PREC, U, 3, true, kNW, true>(a, s);
             return launch_direct_t<FS, PREC, U, 3, false, kNW, true>(a, s);
@@ -351,7 +356,11 @@ int launch_direct(const SpmmArgs& a, int occ, cudaStream_t s) {
         return launch_direct_t<FS, PREC, U, 3, false>(a, s);
     }
     constexpr int U = DirectBatch<FS>::U;
-    if (!epi && env_int("ACCSPMM_ROLL", -1) == 1) return launch_direct_t<FS, PREC, U, 2, false, kNW, true>(a, s);
+    const int roll = env_int("ACCSPMM_ROLL", -1);
+    if (roll < 0 ? kRollDefault<FS, PREC, 2> : roll != 0) {
+        if (epi) return launch_direct_t<FS, PREC, U, 2, true, kNW, true>(a, s);
+        return launch_direct_t<FS, PREC, U, 2, false, kNW, true>(a, s);
+    }
     return epi ? launch_direct_t<FS, PREC, U, 2, true>(a, s) : launch_direct_t<FS, PREC, U, 2, false>(a, s);
 }
 
@@ -391,19 +400,26 @@ int spmm_window_launch(const uint32_t* rwo, const uint32_t* tc_offset, const uin
                        uint32_t T, uint32_t cols, const float* B, float* C, uint32_t K,
                        int precision, cudaStream_t s) {
     return spmm_window_launch_slices(rwo, tc_offset, bits, a2b, vals, W, w_cfg, T, cols, B, C, K,
-                                     precision, 0, 0xFFFFFFFFu, Epilogue{}, s);
+                                     precision, 0, 0xFFFFFFFFu, Epilogue{}, s, 0);
 }
 
 int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, const uint64_t* bits,
                               const uint32_t* a2b, const float* vals, uint32_t W, uint32_t w_cfg,
                               uint32_t T, uint32_t cols, const float* B, float* C, uint32_t K,
                               int precision, uint32_t slice_begin, uint32_t slice_count,
-                              const Epilogue& epi, cudaStream_t s) {
+                              const Epilogue& epi, cudaStream_t s, int slice_fs) {
     if (W == 0) return ACCSPMM_SUCCESS;
     // the launch shape depends only on (w_cfg, T, K, precision), so every
     // entry point cuts a matrix into the same pieces and sums partial windows
     // in the same order
     Config cfg = choose_config(w_cfg, T, K, precision);
+    if (slice_fs && slice_fs != cfg.fs) {
+        // another slice width (the feature columns a CTA covers do not change
+        // any element's arithmetic; the window blocks stay the chooser's)
+        cfg.fs = slice_fs;
+        cfg.kernel = kDirect;
+        cfg.occ = slice_fs == 128 ? 2 : 3;
+    }
     const uint32_t slices = (K + uint32_t(cfg.fs) - 1) / uint32_t(cfg.fs);
     if (slice_begin >= slices) return ACCSPMM_SUCCESS;
     slice_count = std::min(slice_count, slices - slice_begin);
@@ -470,7 +486,7 @@ int spmm_bias_act_impl(const accspmm_metcf_t* m, const float* B, float* C, uint3
     return spmm_window_launch_slices(m->row_window_offset, m->tc_offset, m->tc_local_bit,
                                      m->sparse_a2b, m->data, m->num_windows, m->num_windows,
                                      m->num_tiles, m->cols, B, C, K, precision, 0, 0xFFFFFFFFu, epi,
-                                     as_stream(stream));
+                                     as_stream(stream), 0);
 }
 
 int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uint32_t c_rows,

@@ -3,11 +3,12 @@
 // else.
 //
 // The kernel is the one-matrix register-direct kernel with everything but its
-// B-row gathers taken out: the same work items (window block x feature
-// slice, from the same launch-shape chooser), the same equal per-warp tile
-// pieces, the same lane pattern (eight lanes per 128 contiguous bytes of a
-// row, tile columns tq and tq + 4), the same batch of tiles in flight and
-// the same CTAs per SM -- but no sparse values, no MMAs and no C stores.  The
+// B-row gathers taken out: the same work items (window block x feature slice,
+// from the same launch-shape chooser or at another slice width), the same
+// equal per-warp tile pieces, the same lane pattern (eight lanes per 128
+// contiguous bytes of a row, tile columns tq and tq + 4), the same batch of
+// tiles in flight and the same CTAs per SM -- but no sparse values, no MMAs
+// and no C stores.  The
 // gathered rows are summed into one register so that the loads are not
 // removed.  Its time is what the SpMM would take if its arithmetic, value
 // loads and stores were free: the denominator of the "fraction of the gather
@@ -102,8 +103,8 @@ int launch_floor_shape(const SpmmArgs& a, int fs, int occ, float* sink, cudaStre
 
 }  // namespace
 
-int gather_floor_impl(const accspmm_metcf_t* m, const float* B, uint32_t K, int repeats,
-                      float* avg_ms, void* stream) {
+int gather_floor_impl(const accspmm_metcf_t* m, const float* B, uint32_t K, uint32_t slice_width,
+                      int repeats, float* avg_ms, void* stream) {
     if (!m || m->space != ACCSPMM_DEVICE) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "METCF must be on the device");
     if (!B || K == 0 || K % 4 || (reinterpret_cast<uintptr_t>(B) & 15u))
         ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "B must be a 16-byte aligned device pointer, K a multiple of 4");
@@ -112,6 +113,12 @@ int gather_floor_impl(const accspmm_metcf_t* m, const float* B, uint32_t K, int 
     int fs = 0, occ = 0;
     uint32_t wb = 0;
     launch_shape_for(m->num_windows, m->num_tiles, K, ACCSPMM_PREC_TF32, &fs, &occ, &wb);
+    if (slice_width) {
+        if (slice_width != 32 && slice_width != 64 && slice_width != 128)
+            ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "slice_width must be 0, 32, 64 or 128");
+        fs = int(slice_width);
+        occ = fs == 128 ? 2 : 3;  // the register-direct kernel's CTAs per SM at that width
+    }
     const uint32_t W = m->num_windows;
     SpmmArgs a{m->row_window_offset, m->tc_offset, m->tc_local_bit, m->sparse_a2b, m->data, B,
                nullptr, W, m->cols, K, wb, (K + uint32_t(fs) - 1) / uint32_t(fs), (W + wb - 1) / wb,

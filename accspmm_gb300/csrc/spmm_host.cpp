@@ -2,10 +2,10 @@
 // tf32_spmm / adp_tf32_spmm of src/mma_tf32.cu:12-183 (cudaMalloc, copy B in,
 // launch, copy C out), rebuilt as one pipelined call.
 //
-// The product is cut into the feature slices the launch-shape chooser uses
-// for the device entry points (64 columns at K = 128), so each slice's launch
-// does exactly the arithmetic of the corresponding CTAs of the one-launch
-// entry point and the result is bit-identical to it.  Per slice, on the
+// The product is cut into feature slices of the launch-shape chooser's width,
+// at most 64 columns (two slices at K = 128), each launched with the
+// chooser's window blocks, so every element's arithmetic is that of the
+// one-launch entry point and the result is bit-identical to it.  Per slice, on the
 // library's copy streams:
 //   copy stream 1: B[:, slice] host -> device (a 2D copy of the slice's
 //                  columns), then an event;
@@ -178,7 +178,10 @@ int spmm_host_impl(const accspmm_metcf_t* m, const accspmm_adpbme_t* ad, const f
         rwo = rw;
     }
     const uint32_t w_cfg = W;  // the chooser's key: the matrix's own windows
-    const uint32_t fs = slice_width_for(w_cfg, T, K, precision);
+    // the chooser's slice width, at most 64 columns so that a K > 64 product
+    // has at least two slices to pipeline
+    uint32_t fs = slice_width_for(w_cfg, T, K, precision);
+    if (fs > 64) fs = 64;
     const uint32_t nsl = (K + fs - 1) / fs;
     float* dBf = static_cast<float*>(dB.p);
 
@@ -199,10 +202,10 @@ int spmm_host_impl(const accspmm_metcf_t* m, const accspmm_adpbme_t* ad, const f
         HOST_CUDA(cudaStreamWaitEvent(s, in, 0));
         r = m ? spmm_window_launch_slices(rwo, m->tc_offset, m->tc_local_bit, m->sparse_a2b, m->data,
                                           W, w_cfg, T, cols, dBf, c_dev, K, precision, i, 1,
-                                          Epilogue{}, s)
+                                          Epilogue{}, s, int(fs))
               : spmm_window_launch_slices(rwo, ad->tc_offset, ad->tc_local_bit, ad->sparse_a2b,
                                           ad->data, W, w_cfg, T, cols, dBf, c_dev, K, precision, i,
-                                          1, Epilogue{}, s);
+                                          1, Epilogue{}, s, int(fs));
         if (r) return r;
         if (!direct) {
             cudaEvent_t done;

@@ -27,19 +27,19 @@ struct Epilogue {
 };
 
 // The same launch restricted to feature slices [slice_begin, slice_begin +
-// slice_count) of the chosen slice width: identical arithmetic for the
-// columns it covers.
+// slice_count) of the chosen slice width (or of slice_fs columns when
+// slice_fs is nonzero): identical arithmetic for the columns it covers.
 int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, const uint64_t* bits,
                               const uint32_t* a2b, const float* vals, uint32_t W, uint32_t w_cfg,
                               uint32_t T, uint32_t cols, const float* B, float* C, uint32_t K,
                               int precision, uint32_t slice_begin, uint32_t slice_count,
-                              const Epilogue& epi, cudaStream_t s);
+                              const Epilogue& epi, cudaStream_t s, int slice_fs);
 // Slice width, CTAs per SM (register-direct kernel) and windows per CTA the
 // launch-shape chooser picks.
 void launch_shape_for(uint32_t w_cfg, uint32_t T, uint32_t K, int precision, int* fs, int* occ,
                       uint32_t* wb);
-int gather_floor_impl(const accspmm_metcf_t* m, const float* B, uint32_t K, int repeats,
-                      float* avg_ms, void* stream);
+int gather_floor_impl(const accspmm_metcf_t* m, const float* B, uint32_t K, uint32_t slice_width,
+                      int repeats, float* avg_ms, void* stream);
 // Feature columns per slice the launch-shape chooser picks.
 uint32_t slice_width_for(uint32_t w_cfg, uint32_t T, uint32_t K, int precision);
 // rowWindowOffset of W windows derived from an AdpBME's rowIndices (err: a

@@ -406,12 +406,19 @@ def run_ours(args):
     U = gathered_rows(m) if rank == 0 else None
     if U is not None:
         gbytes = abytes - 4 * n * K + 4 * K * U
-        # the floor: a launch with the same shape that only gathers those rows
-        floor_ms = m.gather_floor(B, K, 10, stream)
+        # the floor: launches that only gather those rows, in the SpMM's own
+        # shape and in the register-direct shapes of the other slice widths;
+        # the fastest is the floor
+        floors = {"spmm_shape": m.gather_floor(B, K, 10, stream)}
+        for w in (32, 64, 128):
+            if w <= max(32, K):
+                floors[str(w)] = m.gather_floor(B, K, 10, stream, slice_width=w)
+        floor_ms = min(floors.values())
         roofline["gather_model"] = {"bytes": int(gbytes), "gathered_rows": U,
                                     "achieved": round(gbytes / (kms * 1e-3) / 1e9, 1),
                                     "frac": round(gbytes / (kms * 1e-3) / 1e9 / peak, 4),
                                     "floor_ms": round(floor_ms, 4),
+                                    "floor_ms_by_shape": {k: round(v, 4) for k, v in floors.items()},
                                     "frac_of_floor": round(floor_ms / kms, 4)}
 
     # end to end through the C ABI with host buffers: accspmm_spmm_host takes

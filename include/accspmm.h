@@ -335,12 +335,15 @@ int accspmm_time_spmm(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp,
 /* Measurement: the gather floor of accspmm_spmm_tf32 on this matrix and B --
  * the average time (one warm-up, then `repeats` launches timed with CUDA
  * events on `stream`) of a kernel that moves exactly the B rows the SpMM
- * kernel gathers, with the SpMM's launch shape, lane pattern and batching,
- * and does nothing else (no sparse values, MMAs or C stores).  The SpMM's
- * time over this floor is how much its arithmetic and bookkeeping cost on
- * top of its unavoidable row gathers.  No counterpart in the reference. */
+ * kernel gathers, with the SpMM's launch shape, lane pattern and batching
+ * (slice_width 0), or with the register-direct shape of another slice width
+ * (32, 64 or 128 columns), and does nothing else (no sparse values, MMAs or
+ * C stores).  The SpMM's time over the fastest floor is how much its
+ * arithmetic and bookkeeping cost on top of its unavoidable row gathers.  No
+ * counterpart in the reference. */
 int accspmm_gather_floor(const accspmm_metcf_t* metcf, const float* B, uint32_t K,
-                         int32_t repeats, float* avg_ms, void* stream);
+                         uint32_t slice_width, int32_t repeats, float* avg_ms,
+                         void* stream);
 
 /* ---- autotuning ----------------------------------------------------------- */
 /* No counterpart in the reference (its launch shape is fixed: warps = K/32 or

@@ -124,6 +124,10 @@ def test_gather_floor_is_a_positive_time_below_the_spmm():
     B = torch_dev(np.random.default_rng(3).uniform(-1, 1, (cols, K)).astype(np.float32))
     floor = m.gather_floor(B, K, 5)
     assert floor > 0
+    for w in (32, 64, 128):
+        assert m.gather_floor(B, K, 3, slice_width=w) > 0
+    with pytest.raises(capi.AccSpmmError):
+        m.gather_floor(B, K, 3, slice_width=48)
     C = empty_dev(m.c_rows, K)
     t = api.time_spmm(m, None, B, C, m.c_rows, K, capi.PREC_TF32, 2, 5)
     assert floor < 1.5 * t
