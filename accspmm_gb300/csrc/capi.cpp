@@ -338,6 +338,7 @@ void accspmm_metcf_destroy(accspmm_metcf_t* m) {
 
 void accspmm_adpbme_destroy(accspmm_adpbme_t* a) {
     if (!a || !a->owned) return;
+    if (a->space == ACCSPMM_DEVICE) adaptive_cache_forget(a);
     free_in(a->space, a->group_offset);
     free_in(a->space, a->tc_offset);
     free_in(a->space, a->row_indices);

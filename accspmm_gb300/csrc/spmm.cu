@@ -489,6 +489,76 @@ int spmm_bias_act_impl(const accspmm_metcf_t* m, const float* B, float* C, uint3
                                      as_stream(stream), 0);
 }
 
+namespace {
+
+// Window offsets derived from the rowIndices of library-owned AdpBME objects,
+// kept per (rowIndices array, window count, device) so that repeated adaptive
+// calls on one object derive them once.  Library-owned arrays are not changed
+// after they are built; accspmm_adpbme_destroy forgets the object's entries.
+struct RwoKey {
+    const uint32_t* ri;
+    uint32_t weff;
+    int dev;
+    bool operator<(const RwoKey& o) const { return std::tie(ri, weff, dev) < std::tie(o.ri, o.weff, o.dev); }
+};
+struct RwoEntry {
+    uint32_t* rwo = nullptr;  // [weff + 2]: offsets, then an error word
+    cudaEvent_t ready = nullptr;
+};
+std::mutex g_rwo_mu;
+std::map<RwoKey, RwoEntry> g_rwo_cache;
+
+// Cached offsets of an owned AdpBME (computed on `s` the first time; later
+// calls on other streams wait for that computation).
+int cached_rwo(const accspmm_adpbme_t* ad, uint32_t Weff, cudaStream_t s, const uint32_t** out) {
+    int dev = 0;
+    ACC_CUDA(cudaGetDevice(&dev));
+    const RwoKey key{ad->row_indices, Weff, dev};
+    std::lock_guard<std::mutex> lock(g_rwo_mu);
+    auto it = g_rwo_cache.find(key);
+    if (it == g_rwo_cache.end()) {
+        RwoEntry e;
+        ACC_CUDA(cudaMalloc(&e.rwo, (size_t(Weff) + 2) * 4));
+        cudaError_t ce = cudaEventCreateWithFlags(&e.ready, cudaEventDisableTiming);
+        if (ce == cudaSuccess) ce = cudaMemsetAsync(e.rwo + Weff + 1, 0, 4, s);
+        if (ce != cudaSuccess) {
+            cudaFree(e.rwo);
+            if (e.ready) cudaEventDestroy(e.ready);
+            ACC_FAIL(ACCSPMM_ERROR_CUDA, "window-offset cache: %s", cudaGetErrorString(ce));
+        }
+        rwo_from_row_indices_kernel<<<(Weff + 1 + 255) / 256, 256, 0, s>>>(ad->row_indices, ad->num_tiles,
+                                                                           Weff, e.rwo, e.rwo + Weff + 1);
+        ce = cudaGetLastError();
+        if (ce == cudaSuccess) ce = cudaEventRecord(e.ready, s);
+        if (ce != cudaSuccess) {
+            cudaStreamSynchronize(s);
+            cudaFree(e.rwo);
+            cudaEventDestroy(e.ready);
+            ACC_FAIL(ACCSPMM_ERROR_CUDA, "window-offset cache: %s", cudaGetErrorString(ce));
+        }
+        it = g_rwo_cache.emplace(key, e).first;
+    } else {
+        ACC_CUDA(cudaStreamWaitEvent(s, it->second.ready, 0));
+    }
+    *out = it->second.rwo;
+    return ACCSPMM_SUCCESS;
+}
+
+}  // namespace
+
+void adaptive_cache_forget(const accspmm_adpbme_t* ad) {
+    std::lock_guard<std::mutex> lock(g_rwo_mu);
+    for (auto it = g_rwo_cache.begin(); it != g_rwo_cache.end();) {
+        if (it->first.ri == ad->row_indices) {
+            cudaFree(it->second.rwo);  // waits for queued work that reads it
+            cudaEventDestroy(it->second.ready);
+            it = g_rwo_cache.erase(it);
+        } else {
+            ++it;
+        }
+    }
+}
+
 int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uint32_t c_rows,
                        uint32_t K, int precision, void* stream) {
     if (!ad || ad->space != ACCSPMM_DEVICE) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "AdpBME must be on the device");
@@ -498,6 +568,14 @@ int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uin
     cudaStream_t s = as_stream(stream);
     const uint32_t Weff = c_rows / kWin, T = ad->num_tiles;
     if (Weff == 0) return ACCSPMM_SUCCESS;
+    if (ad->owned) {
+        const uint32_t* rwo = nullptr;
+        st = cached_rwo(ad, Weff, s, &rwo);
+        if (st) return st;
+        return spmm_window_launch(rwo, ad->tc_offset, ad->tc_local_bit, ad->sparse_a2b, ad->data, Weff,
+                                  (ad->rows + kWin - 1) / kWin, T, ad->cols, B, C, K, precision, s);
+    }
+    // a caller-filled object may change between calls: derive every time
     DevBuf<uint32_t> scratch;  // rwo[Weff + 1] then an error word
     ACC_CUDA(scratch.alloc(size_t(Weff) + 2, s));
     uint32_t* rwo = scratch.p;

@@ -65,6 +65,8 @@ void autotune_clear();
 
 int spmm_tf32_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K, int precision,
                    void* stream);
+// Drops the window offsets cached for an owned AdpBME (before its arrays are freed).
+void adaptive_cache_forget(const accspmm_adpbme_t* ad);
 int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uint32_t c_rows,
                        uint32_t K, int precision, void* stream);
 int device_status_impl(void* stream);

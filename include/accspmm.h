@@ -246,8 +246,11 @@ int accspmm_spmm_tf32(const accspmm_metcf_t* metcf, const float* B, float* C,
  * one launch.  Load balance follows the AdpBME tile order; partial row
  * windows are summed in a fixed order (no float atomics), so the result is
  * deterministic.  C has c_rows rows (accspmm_adaptive_c_rows) and is
- * overwritten, where the reference accumulated into a pre-zeroed C.  Needs
- * 4 (rows/8 + 2) bytes of device scratch, allocated stream-ordered. */
+ * overwritten, where the reference accumulated into a pre-zeroed C.  The
+ * window offsets derived from rowIndices (4 (c_rows/8 + 2) bytes) are kept
+ * with a library-owned AdpBME after its first call, until
+ * accspmm_adpbme_destroy; for an AdpBME the caller filled they are derived
+ * into stream-ordered scratch on every call. */
 int accspmm_spmm_adaptive(const accspmm_adpbme_t* adp, const float* B,
                           float* C, uint32_t c_rows, uint32_t K,
                           int32_t precision, void* stream);

@@ -131,3 +131,27 @@ def test_gather_floor_is_a_positive_time_below_the_spmm():
     C = empty_dev(m.c_rows, K)
     t = api.time_spmm(m, None, B, C, m.c_rows, K, capi.PREC_TF32, 2, 5)
     assert floor < 1.5 * t
+
+
+def test_adaptive_window_offsets_cached_per_object_and_forgotten_on_destroy():
+    # repeated adaptive calls on a library-owned AdpBME reuse its derived
+    # window offsets; destroying it and building another (whose arrays may
+    # land at the same addresses) must not reuse stale offsets
+    K = 64
+    outs = []
+    for name in ("powerlaw40k", "plsym1000", "powerlaw40k", "longwin"):
+        m, cols = device_matrix(name)
+        a = m.adpbme()
+        cr = a.c_rows()
+        B = torch_dev(np.random.default_rng(11).uniform(-1, 1, (cols, K)).astype(np.float32))
+        want = empty_dev(m.c_rows, K)
+        m.spmm(B, want, K)
+        for _ in range(2):
+            got = empty_dev(cr, K)
+            a.spmm(B, got, cr, K)
+            torch.cuda.synchronize()
+            assert torch.equal(got[:m.c_rows], want)
+        outs.append(want.cpu())
+        a.destroy()
+        m.destroy()
+    assert torch.equal(outs[0], outs[2])
