@@ -227,7 +227,7 @@ int rwo_from_row_indices(const uint32_t* ri, uint32_t T, uint32_t W, uint32_t* r
 
 namespace {
 
-enum KernelKind { kDirect = 0, kPipe = 1, kBulk = 2, kLean = 3, kDb = 4 };
+enum KernelKind { kDirect = 0, kPipe = 1, kBulk = 2, kLean = 3, kDb = 4, kTma = 5 };
 
 struct Config {
     int kernel;
@@ -296,6 +296,7 @@ Config choose_config(uint32_t W, uint32_t T, uint32_t K, int precision) {
                    : std::strcmp(e, "bulk") == 0 ? kBulk
                    : std::strcmp(e, "lean") == 0 ? kLean
                    : std::strcmp(e, "db") == 0   ? kDb
+                   : std::strcmp(e, "tma") == 0  ? kTma
                                                  : kDirect;
     int fs = env_int("ACCSPMM_FS", 0);
     if (fs == 32 || fs == 64 || fs == 128) c.fs = fs;
@@ -304,7 +305,7 @@ Config choose_config(uint32_t W, uint32_t T, uint32_t K, int precision) {
     int nw = env_int("ACCSPMM_NW", 0);
     if (nw == 2 || nw == 4 || nw == 8) c.nw = nw;
     if (c.kernel == kPipe && c.fs >= 64) c.nw = 4;  // stage ring must fit in shared memory
-    if (c.kernel == kBulk && c.nw == 8) c.nw = 4;
+    if ((c.kernel == kBulk || c.kernel == kTma) && c.nw == 8) c.nw = 4;
     c.hints = env_int("ACCSPMM_HINTS", c.hints) ? 1 : 0;
     int wbe = env_int("ACCSPMM_WB", 0);
     if (wbe >= 1 && wbe <= 1024) c.wb = uint32_t(wbe);
@@ -430,6 +431,7 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     if (epi.bias || epi.act) cfg.kernel = kDirect;
     if (cfg.kernel == kPipe) return launch_pipe(a, cfg.fs, precision, cfg.nw, cfg.hints, s);
     if (cfg.kernel == kBulk) return launch_bulk(a, cfg.fs, precision, cfg.nw, cfg.hints, s);
+    if (cfg.kernel == kTma) return launch_tma(a, cfg.fs, precision, cfg.nw, s);
     if (cfg.kernel == kLean) return launch_lean(a, cfg.fs, precision, env_int("ACCSPMM_MINB", 4), s);
     if (cfg.kernel == kDb) {
         const bool x3 = precision == ACCSPMM_PREC_3XTF32;

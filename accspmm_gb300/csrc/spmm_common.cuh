@@ -356,6 +356,8 @@ size_t pipe_smem_bytes(int fs, int nw, uint32_t wb);
 // Launch of the bulk-copy (TMA) kernel and its status word (spmm_bulk.cu).
 int launch_bulk(const SpmmArgs& a, int fs, int precision, int nw, int hints, cudaStream_t s);
 int bulk_status(cudaStream_t s, bool clear);
+// Launch of the tensor-map gather4 (TMA) kernel (spmm_bulk.cu).
+int launch_tma(const SpmmArgs& a, int fs, int precision, int nw, cudaStream_t s);
 // Launch of the occupancy-sized register-direct kernel (spmm_lean.cu).
 int launch_lean(const SpmmArgs& a, int fs, int precision, int minb, cudaStream_t s);
 
