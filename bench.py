@@ -402,7 +402,10 @@ def run_ours(args):
                 "peak_source": f"{peak_kind} hbm_gbs", "kernel": "spmm_window_kernel",
                 "kernel_ms": round(kms, 4), "algorithmic_bytes": int(abytes)}
     if traffic:
+        # the DRAM bytes the kernel really moves (ncu, per launch) over its
+        # live time: achieved HBM bandwidth, against the same measured peak
         roofline["dram_gbs"] = round(traffic / (kms * 1e-3) / 1e9, 1)
+        roofline["dram_frac"] = round(traffic / (kms * 1e-3) / 1e9 / peak, 4)
     # gather model (diagnostic): B counted as one K-float row per non-padding
     # sparseA2B entry, i.e. the bytes the kernel must move from L2/HBM to SMs
     U = gathered_rows(m) if rank == 0 else None
