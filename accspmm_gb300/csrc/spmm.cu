@@ -232,7 +232,8 @@ enum KernelKind { kDirect = 0, kPipe = 1, kBulk = 2, kLean = 3, kDb = 4, kTma = 
 struct Config {
     int kernel;
     int fs;
-    int occ;  // register-direct kernel: resident CTAs per SM (2 or 3)
+    int occ;   // register-direct kernel: resident CTAs per SM (2 or 3)
+    int ring;  // register-direct kernel: rolling tile ring (-1 by the default rule, 0 off, 1 on)
     int nw;
     int hints;
     uint32_t wb;
@@ -277,6 +278,7 @@ Config choose_config(uint32_t W, uint32_t T, uint32_t K, int precision) {
     c.kernel = kDirect;
     c.fs = K <= 32 ? 32 : (K <= 64 || precision == ACCSPMM_PREC_3XTF32) ? 64 : 128;
     c.occ = c.fs == 128 ? 2 : 3;
+    c.ring = -1;
     c.nw = c.fs == 32 ? 8 : 4;
     c.hints = 1;
     c.slice_major = 0;
@@ -343,11 +345,11 @@ constexpr bool kRollDefault = PREC == ACCSPMM_PREC_TF32 && ((FS == 64 && MINB ==
 // CTAs per SM; occ = 3: half that batch at 3 CTAs per SM (80 registers a
 // thread), which keeps more warps' gathers in flight per SM.
 template <int FS, int PREC>
-int launch_direct(const SpmmArgs& a, int occ, cudaStream_t s) {
+int launch_direct(const SpmmArgs& a, int occ, int ring, cudaStream_t s) {
     const bool epi = a.bias != nullptr || a.act != 0;
     if (occ == 3) {
         constexpr int U = (DirectBatch<FS>::U + 1) / 2;
-        const int roll = env_int("ACCSPMM_ROLL", -1);
+        const int roll = env_int("ACCSPMM_ROLL", ring);
         const bool use_roll = roll < 0 ? kRollDefault<FS, PREC, 3> : roll != 0;
         if (use_roll) {
             if (epi) return launch_direct_t<FS, PREC, U, 3, true, kNW, true>(a, s);
@@ -357,7 +359,7 @@ int launch_direct(const SpmmArgs& a, int occ, cudaStream_t s) {
         return launch_direct_t<FS, PREC, U, 3, false>(a, s);
     }
     constexpr int U = DirectBatch<FS>::U;
-    const int roll = env_int("ACCSPMM_ROLL", -1);
+    const int roll = env_int("ACCSPMM_ROLL", ring);
     if (roll < 0 ? kRollDefault<FS, PREC, 2> : roll != 0) {
         if (epi) return launch_direct_t<FS, PREC, U, 2, true, kNW, true>(a, s);
         return launch_direct_t<FS, PREC, U, 2, false, kNW, true>(a, s);
@@ -447,9 +449,9 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     const bool x3 = precision == ACCSPMM_PREC_3XTF32;
     const int occ = cfg.occ;
     switch (cfg.fs) {
-        case 32: return x3 ? launch_direct<32, ACCSPMM_PREC_3XTF32>(a, occ, s) : launch_direct<32, ACCSPMM_PREC_TF32>(a, occ, s);
-        case 64: return x3 ? launch_direct<64, ACCSPMM_PREC_3XTF32>(a, occ, s) : launch_direct<64, ACCSPMM_PREC_TF32>(a, occ, s);
-        default: return x3 ? launch_direct<128, ACCSPMM_PREC_3XTF32>(a, occ, s) : launch_direct<128, ACCSPMM_PREC_TF32>(a, occ, s);
+        case 32: return x3 ? launch_direct<32, ACCSPMM_PREC_3XTF32>(a, occ, cfg.ring, s) : launch_direct<32, ACCSPMM_PREC_TF32>(a, occ, cfg.ring, s);
+        case 64: return x3 ? launch_direct<64, ACCSPMM_PREC_3XTF32>(a, occ, cfg.ring, s) : launch_direct<64, ACCSPMM_PREC_TF32>(a, occ, cfg.ring, s);
+        default: return x3 ? launch_direct<128, ACCSPMM_PREC_3XTF32>(a, occ, cfg.ring, s) : launch_direct<128, ACCSPMM_PREC_TF32>(a, occ, cfg.ring, s);
     }
 }
 
@@ -666,8 +668,9 @@ int autotune_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K
     }
     const Config dflt = choose_config(m->num_windows, m->num_tiles, K, precision);
     std::vector<Config> cand;
-    // (kernel, CTAs per SM): register-direct at 3 and 2, double-buffered at 2
-    const int shapes[3][2] = {{kDirect, 3}, {kDirect, 2}, {kDb, 2}};
+    // (kernel, CTAs per SM, tile ring): register-direct at 3 and 2 CTAs per
+    // SM with and without the rolling ring, double-buffered at 2
+    const int shapes[5][3] = {{kDirect, 3, 1}, {kDirect, 3, 0}, {kDirect, 2, 1}, {kDirect, 2, 0}, {kDb, 2, 0}};
     for (const auto& ko : shapes)
         for (int fs : {32, 64, 128}) {
             if (fs > 32 && uint32_t(fs / 2) >= K) continue;  // slices far wider than K
@@ -675,6 +678,7 @@ int autotune_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K
                 Config c = dflt;
                 c.kernel = ko[0];
                 c.occ = ko[1];
+                c.ring = ko[2];
                 c.fs = fs;
                 c.wb = wb;
                 c.slice_major = 0;
@@ -723,6 +727,7 @@ int autotune_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K
     if (out) {
         out->kernel = best.kernel;
         out->ctas_per_sm = best.kernel == kDirect ? uint32_t(best.occ) : 2u;
+        out->tile_ring = best.kernel == kDirect ? (best.ring < 0 ? -1 : best.ring) : 0;
         out->slice_width = uint32_t(best.fs);
         out->windows_per_cta = best.wb;
         out->best_ms = best_ms;

@@ -351,9 +351,10 @@ int accspmm_gather_floor(const accspmm_metcf_t* metcf, const float* B, uint32_t 
 /* ---- autotuning ----------------------------------------------------------- */
 /* No counterpart in the reference (its launch shape is fixed: warps = K/32 or
  * K/64 per CTA, one CTA per window or group).  Times the candidate launch
- * shapes -- kernel variant (register-direct at 3 or 2 CTAs per SM,
- * double-buffered), feature-slice width (32/64/128 columns) and windows per
- * CTA (4/8/16/32, the load-balance granularity) -- on this matrix with this B, and keeps the fastest for the
+ * shapes -- kernel variant (register-direct at 3 or 2 CTAs per SM, with or
+ * without the rolling tile ring that keeps gathers in flight through the
+ * MMAs; double-buffered), feature-slice width (32/64/128 columns) and windows
+ * per CTA (4/8/16/32, the load-balance granularity) -- on this matrix with this B, and keeps the fastest for the
  * matrix's signature (windows, tiles, K, precision) for the rest of the
  * process: later plain, adaptive and batched calls on a matrix with that
  * signature use it.  C is overwritten.  Results of different shapes agree
@@ -367,6 +368,7 @@ typedef struct accspmm_tune_result {
     float default_ms;          /* time of the default shape */
     uint32_t candidates;
     uint32_t ctas_per_sm;      /* resident CTAs per SM of the chosen kernel */
+    int32_t tile_ring;         /* rolling tile ring: 1 on, 0 off, -1 the default rule */
 } accspmm_tune_result_t;
 
 int accspmm_autotune_metcf(const accspmm_metcf_t* metcf, const float* B, float* C,
