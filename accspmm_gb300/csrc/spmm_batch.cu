@@ -6,8 +6,10 @@
 // one-matrix launch -- the window-block size comes from the same chooser -- so
 // each item's arithmetic, and therefore each result, is bit-identical to the
 // matrix's own accspmm_spmm_tf32 launch.  Items are numbered largest matrix
-// first; resident CTAs (three per SM) take items from an atomic counter until
-// none are left, so uneven matrices share the GPU without a tail of idle SMs.
+// first; resident CTAs take items from an atomic counter until none are
+// left, so uneven matrices share the GPU without a tail of idle SMs.  TF32
+// matrices with K > 64 form a second group launched in 128-column slices
+// with the rolling tile ring, their one-matrix default shape.
 // A plan can be captured into a CUDA graph (counter reset + launch) and
 // replayed.
 #include <algorithm>
@@ -77,7 +79,10 @@ spmm_batch_kernel(const BatchDesc* __restrict__ desc, uint32_t n_desc, uint32_t 
 template <int FS, int PREC, bool ROLL>
 int launch_batch_t(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items,
                    uint32_t max_wb, uint32_t* d_counter, cudaStream_t s) {
-    constexpr int kMinB = 3, kU = (DirectBatch<FS>::U + 1) / 2;
+    // 128-column slices: 2 CTAs per SM with the one-matrix kernel's batch;
+    // narrower slices: 3 CTAs per SM with half that batch
+    constexpr int kMinB = FS == 128 ? 2 : 3;
+    constexpr int kU = FS == 128 ? DirectBatch<FS>::U : (DirectBatch<FS>::U + 1) / 2;
     const size_t smem = size_t(2 * kNW * 8 * FS) * 4 + size_t(max_wb + 1) * 4;
     static unsigned attr_set = 0;
     int dev = 0;
@@ -97,8 +102,17 @@ int launch_batch_t(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_item
 
 }  // namespace
 
-// slice width: the one-matrix default (32 columns for K <= 32, else 64)
+// slice width of the narrow group: the one-matrix default (32 columns for
+// K <= 32, else 64)
 int batch_fs_for(uint32_t max_k) { return max_k <= 32 ? 32 : 64; }
+
+bool batch_item_is_wide(uint32_t K, int precision) {
+    static const bool off = [] {
+        const char* e = std::getenv("ACCSPMM_BATCH_WIDE");
+        return e && *e == '0';
+    }();
+    return !off && precision == ACCSPMM_PREC_TF32 && K > 64;
+}
 
 int launch_batch(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items, uint32_t max_wb,
                  uint32_t* d_counter, int fs, int precision, cudaStream_t s) {
@@ -108,6 +122,12 @@ int launch_batch(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items,
     // measured 6 % slower on 128 power-law graphs: off unless ACCSPMM_ROLL=1
     const char* e = std::getenv("ACCSPMM_ROLL");
     const bool roll = e && *e == '1';
+    if (fs == 128) {
+        // wide TF32 items: 128-column slices with the rolling tile ring, the
+        // one-matrix default for K > 64
+        if (x3) ACC_FAIL(ACCSPMM_ERROR_UNSUPPORTED, "128-column batch slices are TF32 only");
+        return launch_batch_t<128, ACCSPMM_PREC_TF32, true>(d_desc, n_desc, total_items, max_wb, d_counter, s);
+    }
     switch (fs) {
         case 32: return x3 ? launch_batch_t<32, ACCSPMM_PREC_3XTF32, false>(d_desc, n_desc, total_items, max_wb, d_counter, s)
                            : launch_batch_t<32, ACCSPMM_PREC_TF32, false>(d_desc, n_desc, total_items, max_wb, d_counter, s);
@@ -164,16 +184,32 @@ int make_batch_descs(const BatchInput* in, uint32_t n, int fs, int precision,
 // ---------------------------------------------------------------------------
 using namespace accspmm;
 
-struct accspmm_batch {
-    int device = 0;
-    int precision = ACCSPMM_PREC_TF32;
+// One persistent launch of a plan: the items of one slice-width class.
+struct BatchGroup {
     int fs = 64;
     uint32_t n_desc = 0, total_items = 0, max_wb = 1;
     BatchDesc* d_desc = nullptr;
     uint32_t* d_counter = nullptr;
+};
+
+// A plan: TF32 items with K > 64 run in 128-column slices with the tile ring
+// (the one-matrix default for them), the others in the narrow shape; one
+// persistent launch per non-empty group, wide group first.
+struct accspmm_batch {
+    int device = 0;
+    int precision = ACCSPMM_PREC_TF32;
+    std::vector<BatchGroup> groups;
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
 };
+
+static void free_groups(accspmm_batch* b) {
+    for (auto& g : b->groups) {
+        cudaFree(g.d_desc);
+        cudaFree(g.d_counter);
+    }
+    b->groups.clear();
+}
 
 extern "C" {
 
@@ -185,37 +221,54 @@ int accspmm_batch_create(const accspmm_batch_item_t* items, uint32_t n, int32_t 
         ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "unknown precision %d", precision);
     *out = nullptr;
     std::vector<BatchInput> in(n);
-    uint32_t max_k = 4;
     for (uint32_t i = 0; i < n; ++i) {
         const accspmm_metcf_t* m = items[i].metcf;
         if (!m || m->space != ACCSPMM_DEVICE) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "item %u: METCF must be on the device", i);
         in[i] = BatchInput{m->row_window_offset, m->tc_offset, m->tc_local_bit, m->sparse_a2b, m->data,
                            items[i].B, items[i].C, m->num_windows, m->num_windows, m->num_tiles,
                            m->cols, items[i].K};
-        max_k = std::max(max_k, items[i].K);
     }
     auto* b = new accspmm_batch();
     cudaGetDevice(&b->device);
     b->precision = precision;
-    b->fs = batch_fs_for(max_k);
-    std::vector<BatchDesc> d;
-    int st = make_batch_descs(in.data(), n, b->fs, precision, &d, &b->total_items, &b->max_wb);
-    if (st) {
-        delete b;
-        return st;
+    // split by slice-width class, keeping each item's position for its index
+    std::vector<BatchInput> cls[2];
+    std::vector<uint32_t> pos[2];
+    uint32_t narrow_k = 4;
+    for (uint32_t i = 0; i < n; ++i) {
+        const int c = batch_item_is_wide(in[i].K, precision) ? 0 : 1;
+        cls[c].push_back(in[i]);
+        pos[c].push_back(i);
+        if (c == 1) narrow_k = std::max(narrow_k, in[i].K);
     }
-    b->n_desc = uint32_t(d.size());
-    if (cudaMalloc(&b->d_desc, sizeof(BatchDesc) * std::max<size_t>(1, d.size())) != cudaSuccess ||
-        cudaMalloc(&b->d_counter, 4) != cudaSuccess) {
-        cudaFree(b->d_desc);
-        delete b;
-        ACC_FAIL(ACCSPMM_ERROR_ALLOC, "device allocation of the batch table failed");
-    }
-    if (!d.empty() && cudaMemcpy(b->d_desc, d.data(), sizeof(BatchDesc) * d.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
-        cudaFree(b->d_desc);
-        cudaFree(b->d_counter);
-        delete b;
-        ACC_FAIL(ACCSPMM_ERROR_CUDA, "copy of the batch table failed");
+    for (int c = 0; c < 2; ++c) {
+        if (cls[c].empty()) continue;
+        BatchGroup g;
+        g.fs = c == 0 ? 128 : batch_fs_for(narrow_k);
+        std::vector<BatchDesc> d;
+        int st = make_batch_descs(cls[c].data(), uint32_t(cls[c].size()), g.fs, precision, &d,
+                                  &g.total_items, &g.max_wb);
+        if (st) {
+            free_groups(b);
+            delete b;
+            return st;
+        }
+        for (auto& x : d) x.index = pos[c][x.index];
+        g.n_desc = uint32_t(d.size());
+        if (cudaMalloc(&g.d_desc, sizeof(BatchDesc) * std::max<size_t>(1, d.size())) != cudaSuccess ||
+            cudaMalloc(&g.d_counter, 4) != cudaSuccess) {
+            cudaFree(g.d_desc);
+            free_groups(b);
+            delete b;
+            ACC_FAIL(ACCSPMM_ERROR_ALLOC, "device allocation of the batch table failed");
+        }
+        b->groups.push_back(g);
+        if (!d.empty() &&
+            cudaMemcpy(g.d_desc, d.data(), sizeof(BatchDesc) * d.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+            free_groups(b);
+            delete b;
+            ACC_FAIL(ACCSPMM_ERROR_CUDA, "copy of the batch table failed");
+        }
     }
     *out = b;
     return ACCSPMM_SUCCESS;
@@ -224,9 +277,13 @@ int accspmm_batch_create(const accspmm_batch_item_t* items, uint32_t n, int32_t 
 int accspmm_batch_run(accspmm_batch_t* b, void* stream) {
     clear_error();
     if (!b) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "null batch");
-    if (b->total_items == 0) return ACCSPMM_SUCCESS;
-    return launch_batch(b->d_desc, b->n_desc, b->total_items, b->max_wb, b->d_counter, b->fs,
-                        b->precision, as_stream(stream));
+    for (const auto& g : b->groups) {
+        if (g.total_items == 0) continue;
+        const int st = launch_batch(g.d_desc, g.n_desc, g.total_items, g.max_wb, g.d_counter, g.fs,
+                                    b->precision, as_stream(stream));
+        if (st) return st;
+    }
+    return ACCSPMM_SUCCESS;
 }
 
 int accspmm_batch_capture(accspmm_batch_t* b, void* stream) {
@@ -270,9 +327,15 @@ int accspmm_batch_info(const accspmm_batch_t* b, uint32_t* n_items, uint32_t* wo
                        uint32_t* slice_width) {
     clear_error();
     if (!b) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "null batch");
-    if (n_items) *n_items = b->n_desc;
-    if (work_items) *work_items = b->total_items;
-    if (slice_width) *slice_width = uint32_t(b->fs);
+    uint32_t n = 0, w = 0, fs = 0;
+    for (const auto& g : b->groups) {
+        n += g.n_desc;
+        w += g.total_items;
+        fs = std::max<uint32_t>(fs, uint32_t(g.fs));
+    }
+    if (n_items) *n_items = n;
+    if (work_items) *work_items = w;
+    if (slice_width) *slice_width = fs;
     return ACCSPMM_SUCCESS;
 }
 
@@ -280,8 +343,7 @@ void accspmm_batch_destroy(accspmm_batch_t* b) {
     if (!b) return;
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
-    cudaFree(b->d_desc);
-    cudaFree(b->d_counter);
+    free_groups(b);
     delete b;
 }
 

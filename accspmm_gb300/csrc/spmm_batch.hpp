@@ -42,8 +42,10 @@ struct BatchInput {
     uint32_t K;
 };
 
-// Slice width of a launch whose widest matrix has max_k columns.
+// Slice width of a narrow-group launch whose widest matrix has max_k columns.
 int batch_fs_for(uint32_t max_k);
+// Whether a batch item runs in the wide group (128-column slices, tile ring).
+bool batch_item_is_wide(uint32_t K, int precision);
 
 // Descriptors in launch order (largest first), with item numbering.
 int make_batch_descs(const BatchInput* in, uint32_t n, int fs, int precision,
