@@ -703,7 +703,7 @@ def run_serve(args):
     # outputs: one page-locked arena from which each request takes exactly its
     # C (c_rows x K floats) and returns it when done, so the number of
     # requests in flight is bounded by bytes, not by worst-case slots
-    arena_floats = (24 << 30) // 4
+    arena_floats = min(24 << 30, max_rows * 512 * 4 * 64) // 4
     arena = torch.empty((arena_floats,), dtype=torch.float32, pin_memory=True)
     prec = capi.PREC_3XTF32 if args.precision == "3xtf32" else capi.PREC_TF32
 

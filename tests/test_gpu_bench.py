@@ -1,0 +1,51 @@
+"""bench.py's GPU workloads at small sizes: each prints one JSON line with the
+fields the measurement contract needs (the full-size runs are what bench.py
+reports; these keep every mode working)."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def run(*args, timeout=600):
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *args], capture_output=True,
+                       text=True, timeout=timeout, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1, r.stdout[-2000:]
+    return json.loads(lines[0])
+
+
+def test_scale_mode_small():
+    d = run("--n", "65536", "--k", "64", "--steps", "5", "--warmup", "3", "--no-sweep",
+            "--no-host-build", "--no-autotune")
+    assert d["value"] > 0 and d["ms_per_step"] > 0 and d["gpu_launches"] == 5
+    for key in ("roofline", "cpu_baseline", "e2e", "clocks", "comparators"):
+        assert d[key] is not None, key
+    assert d["roofline"]["bound"] == "hbm" and 0 < d["roofline"]["frac"]
+    assert d["e2e"]["h2d_bytes_per_step"] == 65536 * 64 * 4
+    assert d["roofline"]["gather_model"]["floor_ms"] > 0
+
+
+def test_batch_mode_small():
+    d = run("--workload", "batch", "--graphs", "12", "--rows-hi", "5000", "--steps", "2",
+            "--warmup", "3")
+    assert d["batch"]["bitwise_equal_to_separate"] is True
+    assert d["config"]["graphs"] == 12 and d["value"] > 0
+
+
+def test_precision_mode_small():
+    d = run("--workload", "precision", "--n", "131072")
+    assert d["targets"]["tf32_rel_fro_le_1e-3"] and d["targets"]["3xtf32_rel_fro_le_1e-6"]
+
+
+def test_serve_mode_small():
+    d = run("--workload", "serve", "--rows-hi", "8000", timeout=900)
+    cb = d["serve"]["continuous_batching"]
+    assert all(v["achieved_rps"] > 0 and v["p99_ms"] >= v["p50_ms"] for v in cb.values())
