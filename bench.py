@@ -58,6 +58,8 @@ def parse():
                    help="scale: the 1M-row SpMM (headline); batch: many graphs in one "
                         "launch vs one launch each; precision: TF32 vs 3xTF32 vs FP64")
     p.add_argument("--graphs", type=int, default=512)
+    p.add_argument("--chains", type=float, default=0.0,
+                   help="serve workload: fraction of requests that are two-layer chains A (A B)")
     p.add_argument("--rows-hi", type=int, default=0,
                    help="largest graph rows of the batch / serve workloads (default: the "
                         "stated 200,000 for batch, 500,000 for serve)")
@@ -745,6 +747,7 @@ def run_serve(args):
         arr = np.cumsum(rng.exponential(1.0 / rate, size=n_req))
         g_of = rng.integers(0, n_graphs, size=n_req)
         k_of = rng.choice(ks, size=n_req)
+        chain_of = np.where(rng.random(n_req) < args.chains, 2, 1)
         ids = [None] * n_req
         pool = Arena(arena_floats)
 
@@ -766,7 +769,7 @@ def run_serve(args):
                 time.sleep(wait_s)
             g, k = int(g_of[i]), int(k_of[i])
             off, size = pool.get(graphs[g].c_rows * k)
-            rid = srv.submit(g, Bh, arena[off:off + size], k, prec)
+            rid = srv.submit(g, Bh, arena[off:off + size], k, prec, int(chain_of[i]))
             ids[i] = (rid, off, size)
         th.join()
         return srv.stats()
@@ -800,6 +803,7 @@ def run_serve(args):
                                "copied from pinned host memory per request, C copied back, "
                                "HBM budget 150 GB",
                    "output_arena_gb": arena_floats * 4 / (1 << 30),
+                   "two_layer_chain_fraction": args.chains,
                    "graph_rows": int(sum(g.struct.rows for g in graphs)),
                    "graph_nnz": int(sum(g.struct.nnz for g in graphs))},
         "serve": results,
