@@ -2,9 +2,9 @@
 // tf32_spmm / adp_tf32_spmm of src/mma_tf32.cu:12-183 (cudaMalloc, copy B in,
 // launch, copy C out), rebuilt as one pipelined call.
 //
-// The product is cut into feature slices of the launch-shape chooser's width,
-// at most 64 columns (two slices at K = 128), each launched with the
-// chooser's window blocks, so every element's arithmetic is that of the
+// The product is cut into feature slices of the launch-shape chooser's width
+// cut to about a quarter of K, 32 to 64 columns (four slices at K = 128 and
+// K = 256), each launched with the chooser's window blocks, so every element's arithmetic is that of the
 // one-launch entry point and the result is bit-identical to it.  Per slice, on the
 // library's copy streams:
 //   copy stream 1: B[:, slice] host -> device (a 2D copy of the slice's
@@ -20,6 +20,8 @@
 // repeated calls do not map and unmap device memory.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -178,10 +180,18 @@ int spmm_host_impl(const accspmm_metcf_t* m, const accspmm_adpbme_t* ad, const f
         rwo = rw;
     }
     const uint32_t w_cfg = W;  // the chooser's key: the matrix's own windows
-    // the chooser's slice width, at most 64 columns so that a K > 64 product
-    // has at least two slices to pipeline
+    // the chooser's slice width, cut to about a quarter of K (at least 32,
+    // at most 64 columns): on the 1M-row power-law matrix four slices
+    // pipelined the link transfers better than two (K = 128: 4.40 against
+    // 4.67 ms; K = 64, two slices of 32: 2.37 against 2.77 ms for one), and
+    // slices narrower than 64 columns at K = 256 repeated too much of the
+    // per-tile work (8 slices of 32: 11.4 ms, 4 of 64: 8.2 ms)
     uint32_t fs = slice_width_for(w_cfg, T, K, precision);
+    fs = std::min(fs, std::max<uint32_t>(32u, (K / 4u) / 32u * 32u));
     if (fs > 64) fs = 64;
+    const char* fs_str = std::getenv("ACCSPMM_HOST_FS");  // measurement override
+    const int fs_env = fs_str ? std::atoi(fs_str) : 0;
+    if (fs_env == 32 || fs_env == 64 || fs_env == 128) fs = uint32_t(fs_env);
     const uint32_t nsl = (K + fs - 1) / fs;
     float* dBf = static_cast<float*>(dB.p);
 

@@ -49,14 +49,18 @@ def parse():
     p.add_argument("--precision", default="tf32", choices=["tf32", "3xtf32"])
     p.add_argument("--no-sweep", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-ref-gpu", action="store_true",
+                   help="reference arm: skip timing the reference's own GPU kernels")
     p.add_argument("--no-host-build", action="store_true")
     p.add_argument("--no-cusparse", action="store_true",
                    help="skip the cuSPARSE CSR SpMM comparator (torch.sparse, FP32)")
     p.add_argument("--no-autotune", action="store_true",
                    help="time the default launch shape instead of the autotuned one")
-    p.add_argument("--workload", default="scale", choices=["scale", "batch", "precision", "serve"],
+    p.add_argument("--workload", default="scale", choices=["scale", "batch", "precision", "serve", "small"],
                    help="scale: the 1M-row SpMM (headline); batch: many graphs in one "
-                        "launch vs one launch each; precision: TF32 vs 3xTF32 vs FP64")
+                        "launch vs one launch each; precision: TF32 vs 3xTF32 vs FP64; "
+                        "serve: Poisson requests against resident graphs; small: the "
+                        "16,384-row symmetric matrix, with and without L2 flushes")
     p.add_argument("--graphs", type=int, default=512)
     p.add_argument("--chains", type=float, default=0.0,
                    help="serve workload: fraction of requests that are two-layer chains A (A B)")
@@ -242,13 +246,35 @@ def cpu_baseline(rp, ci, v, B, budget_s=8.0):
                       f"FP32 CSR SpMM, OpenMP over rows"}
 
 
+def small_workload(seed: int):
+    """The 16,384-row symmetric power-law matrix (full symmetric COO)."""
+    from accspmm_gb300 import synth
+    return synth.expand_symmetric(*synth.powerlaw_symmetric(n=16384, seed=seed))
+
+
+def small_workload_name(k):
+    return (f"powerlaw_symmetric N=16384 (lower triangle expanded), mean degree 16 "
+            f"before symmetrisation, B=N x {k} fp32 uniform[-1,1)")
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    rp, ci, v = workload(args.n, args.seed)
-    B = np.random.default_rng(args.seed + 7).uniform(-1, 1, (args.n, args.k)).astype(np.float32)
     from oracle import oracle
+    if args.workload == "small":
+        r, c, vv = small_workload(args.seed)
+        args.n = 16384
+        rp, ci, v = oracle.csr_from_coo(args.n, r, c, vv)
+        wname = small_workload_name(args.k)
+    elif args.workload == "scale":
+        rp, ci, v = workload(args.n, args.seed)
+        wname = workload_name(args.n, args.k)
+    else:
+        print(json.dumps({"impl": "reference", "unavailable": f"no reference arm for the {args.workload} "
+                          "workload (the reference has no batched or served path)"}))
+        return
+    B = np.random.default_rng(args.seed + 7).uniform(-1, 1, (args.n, args.k)).astype(np.float32)
     threads = oracle.omp_max_threads()
     C = np.zeros((args.n, args.k), np.float32)
     t0 = time.perf_counter()
@@ -280,14 +306,54 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
         "data": "synthetic", "impl": "reference",
-        "config": {"workload": workload_name(args.n, args.k), "n_rows": args.n, "nnz": int(len(ci)),
+        "config": {"workload": wname, "n_rows": args.n, "nnz": int(len(ci)),
                    "K": args.k, "path": "CPU CSR SpMM (oracle port; the reference has no CPU SpMM)"},
         "cpu_baseline": {"value": round(gf, 2), "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{rows_per_step} consecutive rows per step (of {args.n}), "
                                    f"{args.steps} steps"},
         "e2e": {"value": round(gf, 2), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if not args.no_ref_gpu:
+        out["reference_gpu_kernels"] = reference_gpu(args, rp, ci, v)
     print(json.dumps(out))
+
+
+def reference_gpu(args, rp, ci, v):
+    """The reference's own SpMM kernels (include/mma_tf32.cuh compiled for
+    sm_103a from its sources) on this GPU, on the same matrix, timed with the
+    reference's method: the kernel its driver picks for the matrix (the
+    balance decision), per K, and its plain kernel at the bench's K.  The
+    METCF/AdpBME arrays come from the oracle's restatement of the reference's
+    host builders.  Reported beside the CPU number, not as the arm's value."""
+    from oracle import oracle, ref_gpu
+    why = ref_gpu.available()
+    if why:
+        return {"unavailable": why}
+    import torch
+    n, nnz = args.n, int(len(ci))
+    m = oracle.metcf(n, rp, ci, v)
+    adaptive = bool(oracle.balance_strategy(m["rwo"]))
+    groups = oracle.adpbme_groups(m["rwo"]) if adaptive else None
+    ri = oracle.adpbme_row_indices(m["rwo"]) if adaptive else None
+    ker = ref_gpu.RefKernels()
+    gen = torch.Generator(device="cuda").manual_seed(args.seed)
+    ks = sorted({args.k} | (set() if args.no_sweep else {32, 64, 128, 256}))
+    by_k, plain_by_k = {}, {}
+    for K in ks:
+        B = torch.rand((n, K), device="cuda", generator=gen) * 2 - 1
+        r = ref_gpu.time_reference_path(m, n, B, K, adaptive, groups, ri, ker)
+        r["gflops"] = round(2.0 * nnz * K / (r["ms"] * 1e-3) / 1e9, 1)
+        by_k[str(K)] = r
+        if adaptive:
+            # the plain kernel reads every column of each gathered B row
+            p = ref_gpu.time_reference_path(m, n, B, K, False, kernels=ker)
+            p["gflops"] = round(2.0 * nnz * K / (p["ms"] * 1e-3) / 1e9, 1)
+            plain_by_k[str(K)] = p
+        del B
+    return {"path": "adaptive" if adaptive else "plain", "by_k": by_k, "plain_kernel_by_k": plain_by_k,
+            "timing": "10 warm-up + 10 timed launches, events on the default stream (the reference's loop)",
+            "note": "the reference's kernels compute A*B only for identical B rows and K >= 64; "
+                    "its balance kernels read B columns 0-31 (0-63 above K = 128) in every warp"}
 
 
 def run_ours(args):
@@ -509,6 +575,92 @@ def run_ours(args):
     print(json.dumps(out))
     if world > 1:
         dist.destroy_process_group()
+
+
+def run_small(args):
+    """The 16,384-row symmetric power-law matrix at K = 128: L2-resident
+    (about 21 MB of compulsory bytes), so each SpMM is a few microseconds and
+    launch overhead shows.  Timed twice: back to back (the reference's loop of
+    warm-up then timed launches) and with L2 flushed before every step (a
+    256 MB buffer written between steps, each step bracketed by its own
+    events)."""
+    import torch
+
+    from accspmm_gb300 import api, capi
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    prec = capi.PREC_3XTF32 if args.precision == "3xtf32" else capi.PREC_TF32
+    n, K = 16384, args.k
+    r, c, v = small_workload(args.seed)
+    csr = api.csr_from_coo(n, n, r, c, v)
+    nnz = int(csr["nnz"])
+    stream = torch.cuda.current_stream()
+    m = api.DeviceMETCF.from_csr(api.DeviceCSR.upload(csr, stream), stream)
+    adaptive = m.balance_strategy(stream)
+    adp = m.adpbme(stream=stream) if adaptive else None
+    c_rows = adp.c_rows(stream) if adaptive else m.c_rows
+    gen = torch.Generator(device=dev).manual_seed(args.seed)
+    B = torch.rand((n, K), device=dev, generator=gen) * 2 - 1
+    C = torch.empty((c_rows, K), device=dev)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)  # 256 MB > L2
+
+    def step():
+        if adaptive:
+            adp.spmm(B, C, c_rows, K, prec, stream)
+        else:
+            m.spmm(B, C, K, prec, stream)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        warm_ms = e0.elapsed_time(e1) / args.steps
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        for a, b in evs:
+            flush.fill_(1.0)
+            a.record(stream)
+            step()
+            b.record(stream)
+        torch.cuda.synchronize()
+    cold_ms = statistics.mean(a.elapsed_time(b) for a, b in evs)
+    flops = 2.0 * nnz * K
+    T, W = m.struct.num_tiles, m.struct.num_windows
+    G = adp.struct.num_groups if adaptive else None
+    abytes = algorithmic_bytes(nnz, T, W, n, K, G)
+    peak, peak_kind = peaks()
+    cpu = None
+    if not args.no_cpu_baseline:
+        rp, ci, vv = csr["row_ptr"], csr["col_idx"], csr["data"]
+        cpu = cpu_baseline(rp, ci, vv, B.cpu().numpy(), budget_s=2.0)
+    out = {
+        "metric": METRIC, "value": round(flops / (cold_ms * 1e-3) / 1e9, 2), "unit": UNIT,
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(cold_ms, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": args.precision, "data": "synthetic",
+        "config": {"workload": small_workload_name(K),
+                   "n_rows": n, "nnz": nnz, "K": K, "tiles": int(T), "windows": int(W), "groups": G,
+                   "path": "adaptive" if adaptive else "plain",
+                   "l2": "flushed before every timed step (256 MB written)"},
+        "no_flush": {"ms_per_step": round(warm_ms, 5),
+                     "value": round(flops / (warm_ms * 1e-3) / 1e9, 2),
+                     "timing": "back-to-back launches, one event pair around the loop"},
+        "roofline": {"bound": "hbm", "achieved": round(abytes / (cold_ms * 1e-3) / 1e9, 1),
+                     "peak": peak, "unit": "GB/s",
+                     "frac": round(abytes / (cold_ms * 1e-3) / 1e9 / peak, 4),
+                     "traffic": None, "peak_source": f"{peak_kind} hbm_gbs",
+                     "algorithmic_bytes": int(abytes)},
+        "cpu_baseline": cpu,
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(out))
 
 
 def batch_workload(n_graphs: int, seed: int, row_lo: int = 1000, row_hi: int = 20000):
@@ -822,6 +974,8 @@ def main():
         run_serve(args)
     elif args.workload == "precision":
         run_precision(args)
+    elif args.workload == "small":
+        run_small(args)
     else:
         run_ours(args)
 

@@ -49,3 +49,22 @@ def test_serve_mode_small():
     d = run("--workload", "serve", "--rows-hi", "8000", timeout=900)
     cb = d["serve"]["continuous_batching"]
     assert all(v["achieved_rps"] > 0 and v["p99_ms"] >= v["p50_ms"] for v in cb.values())
+
+
+def test_small_mode():
+    d = run("--workload", "small", "--steps", "20", "--warmup", "5")
+    assert d["config"]["n_rows"] == 16384 and d["gpu_launches"] == 20
+    assert d["ms_per_step"] > 0 and d["no_flush"]["ms_per_step"] > 0
+    assert d["cpu_baseline"]["value"] > 0 and d["roofline"]["frac"] > 0
+
+
+def test_reference_arm_gpu_kernels():
+    from oracle import ref_gpu
+    if not __import__("os").path.exists(ref_gpu.CUBIN):
+        pytest.skip("reference kernels not built here")
+    d = run("--impl", "reference", "--n", "65536", "--k", "64", "--steps", "2", "--warmup", "1")
+    g = d["reference_gpu_kernels"]
+    assert "unavailable" not in g, g
+    assert g["by_k"]["64"]["ms"] > 0
+    assert g["path"] == "plain" or g["plain_kernel_by_k"]["64"]["ms"] > 0
+    assert d["value"] > 0 and d["impl"] == "reference"
