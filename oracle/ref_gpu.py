@@ -117,6 +117,19 @@ def _upload(a: np.ndarray, pad_value=0):
     return torch.from_numpy(ext.view(signed[a.dtype])).cuda()
 
 
+def launch_config(K: int, adaptive: bool, W: int, G: int | None = None):
+    """(kernel name, grid, block) the reference's driver uses: TF32Compute
+    with threshold 512 on the plain path and 128 on the adaptive path
+    (src/mma_tf32.cu:218, include/tf32_comp.hpp:19-31, 52-111)."""
+    threshold = 128 if adaptive else 512
+    warps = K // 32 if K <= threshold else K // 64
+    if adaptive:
+        name = "tf32_mma_balance_kernel" if K <= threshold else "tf32_mma_balance_g128_kernel"
+        return name, int(G), (32, warps)
+    name = "tf32_mma_kernel" if K <= threshold else "tf32_mma_g512_kernel"
+    return name, int(W), (32, warps)
+
+
 def time_reference_path(m: dict, rows: int, B, K: int, adaptive: bool, groups=None, row_indices=None,
                         kernels: RefKernels | None = None) -> dict:
     """Average ms per launch of the kernel the reference's driver runs for
@@ -124,7 +137,7 @@ def time_reference_path(m: dict, rows: int, B, K: int, adaptive: bool, groups=No
     rows = cols), B a CUDA float32 tensor of rows x K."""
     import torch
     assert B.is_cuda and B.dtype == torch.float32 and tuple(B.shape) == (rows, K) and B.is_contiguous()
-    assert K % 32 == 0 and 32 <= K <= 512 and rows * K < 2 ** 32
+    assert K % 32 == 0 and 32 <= K <= 512 and rows * K < 2 ** 32  # tf32_mma_g512_kernel not loaded
     a2b = m["a2b"]
     assert ((a2b < rows) | (a2b == PAD)).all()
     ker = kernels or RefKernels()
@@ -134,24 +147,20 @@ def time_reference_path(m: dict, rows: int, B, K: int, adaptive: bool, groups=No
     p = lambda t: C.c_uint64(t.data_ptr())  # noqa: E731
     Bp = C.c_uint64(B.data_ptr())
     if not adaptive:
-        name = "tf32_mma_kernel"
-        block = (32, K // 32)
+        name, grid, block = launch_config(K, False, W)
         Cd = torch.zeros((8 * W + 8, K), device="cuda")
         args = [p(d["bits"]), p(d["a2b"]), p(d["data"]), p(d["rwo"]), p(d["tco"]), Bp, p(Cd),
                 C.c_uint32(rows), C.c_uint32(K)]
-        grid = W
     else:
         assert groups is not None and row_indices is not None and len(groups) >= 2
         G = len(groups) - 1
-        name = "tf32_mma_balance_kernel" if K <= 128 else "tf32_mma_balance_g128_kernel"
-        block = (32, K // 32) if K <= 128 else (32, K // 64)
+        name, grid, block = launch_config(K, True, W, G)
         c_rows = max(8 * G, int(row_indices[-1]) + 8)
         Cd = torch.zeros((c_rows + 8, K), device="cuda")
         go = _upload(groups, groups[-1])
         ri = _upload(row_indices, row_indices[-1])
         args = [p(go), p(d["tco"]), p(ri), p(d["bits"]), p(d["a2b"]), p(d["data"]), Bp, p(Cd),
                 C.c_uint32(rows), C.c_uint32(K)]
-        grid = G
     torch.cuda.synchronize()
     ms = ker._time(ker.fn[name], grid, block, args)
     torch.cuda.synchronize()

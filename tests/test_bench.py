@@ -61,3 +61,18 @@ def test_replica_throughput_takes_the_slowest_rank_over_gloo():
         assert ms == pytest.approx(4.0)
         assert gf == pytest.approx(2e9 * 2 / 4e-3 / 1e9)
     assert bench.replica_throughput(2.0, 2e9, 1) == (2.0, pytest.approx(1000.0))
+
+
+def test_reference_kernel_launch_config():
+    """The reference's TF32Compute choices (include/tf32_comp.hpp:19-31,
+    52-111; thresholds 512 plain and 128 adaptive, src/mma_tf32.cu:218)."""
+    from oracle import ref_gpu
+    assert ref_gpu.launch_config(128, False, 131072) == ("tf32_mma_kernel", 131072, (32, 4))
+    assert ref_gpu.launch_config(256, False, 10) == ("tf32_mma_kernel", 10, (32, 8))
+    assert ref_gpu.launch_config(1024, False, 10) == ("tf32_mma_g512_kernel", 10, (32, 16))
+    assert ref_gpu.launch_config(32, True, 10, 7) == ("tf32_mma_balance_kernel", 7, (32, 1))
+    assert ref_gpu.launch_config(128, True, 10, 7) == ("tf32_mma_balance_kernel", 7, (32, 4))
+    assert ref_gpu.launch_config(256, True, 10, 7) == ("tf32_mma_balance_g128_kernel", 7, (32, 4))
+    import torch
+    if not torch.cuda.is_available():
+        assert ref_gpu.available() is not None
