@@ -328,6 +328,7 @@ void accspmm_csr_destroy(accspmm_csr_t* c) {
 
 void accspmm_metcf_destroy(accspmm_metcf_t* m) {
     if (!m || !m->owned) return;
+    if (m->space == ACCSPMM_DEVICE) schedule_cache_forget(m->row_window_offset);
     free_in(m->space, m->row_window_offset);
     free_in(m->space, m->tc_offset);
     free_in(m->space, m->tc_local_bit);

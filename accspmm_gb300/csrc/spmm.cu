@@ -216,7 +216,119 @@ __global__ void rwo_from_row_indices_kernel(const uint32_t* __restrict__ ri, uin
     if (w < Weff && lo < T && lo > 0 && ri[lo] < ri[lo - 1]) atomicOr(err, 2u);
 }
 
+// Heaviest-first schedule of nb window blocks of wb windows: order[i] = the
+// block with the i-th largest tile count (ties by block index).  One CTA
+// sorts (~tiles, block) keys with a bitonic network in shared memory;
+// P = nb rounded up to a power of two, at most kOrderMaxBlocks.
+constexpr uint32_t kOrderMaxBlocks = 4096;
+constexpr uint32_t kOrderMaxWaves = 6;  // launches of at most this many waves of CTAs
+
+__global__ void __launch_bounds__(1024) block_order_kernel(const uint32_t* __restrict__ rwo, uint32_t W,
+                                                           uint32_t wb, uint32_t nb, uint32_t P,
+                                                           uint32_t* __restrict__ order) {
+    extern __shared__ unsigned long long s_keys[];
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+        unsigned long long k = ~0ull;
+        if (i < nb) {
+            const uint32_t w0 = i * wb, w1 = min(w0 + wb, W);
+            const uint32_t tiles = rwo[w1] - rwo[w0];
+            k = (static_cast<unsigned long long>(~tiles) << 32) | i;
+        }
+        s_keys[i] = k;
+    }
+    __syncthreads();
+    for (uint32_t k = 2; k <= P; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+                const uint32_t ixj = i ^ j;
+                if (ixj > i) {
+                    const unsigned long long x = s_keys[i], y = s_keys[ixj];
+                    if ((x > y) == ((i & k) == 0)) {
+                        s_keys[i] = y;
+                        s_keys[ixj] = x;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) order[i] = uint32_t(s_keys[i]);
+}
+
+// Heaviest-first schedules of library-owned matrices, per (window offsets,
+// windows, windows per block, device); computed on the calling stream the
+// first time, later calls on other streams wait for that computation.
+struct OrderKey {
+    const uint32_t* rwo;
+    uint32_t W, wb;
+    int dev;
+    bool operator<(const OrderKey& o) const {
+        return std::tie(rwo, W, wb, dev) < std::tie(o.rwo, o.W, o.wb, o.dev);
+    }
+};
+struct OrderEntry {
+    uint32_t* order = nullptr;
+    cudaEvent_t ready = nullptr;
+};
+std::mutex g_order_mu;
+std::map<OrderKey, OrderEntry> g_order_cache;
+
+int cached_order(const uint32_t* rwo, uint32_t W, uint32_t wb, uint32_t nb, cudaStream_t s,
+                 const uint32_t** out) {
+    int dev = 0;
+    ACC_CUDA(cudaGetDevice(&dev));
+    const OrderKey key{rwo, W, wb, dev};
+    std::lock_guard<std::mutex> lock(g_order_mu);
+    auto it = g_order_cache.find(key);
+    if (it != g_order_cache.end()) {
+        ACC_CUDA(cudaStreamWaitEvent(s, it->second.ready, 0));
+        *out = it->second.order;
+        return ACCSPMM_SUCCESS;
+    }
+    // a stream being captured into a graph may not allocate: keep the
+    // launch order there (same results) until a call outside a capture
+    // has built the schedule
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    ACC_CUDA(cudaStreamIsCapturing(s, &cs));
+    if (cs != cudaStreamCaptureStatusNone) {
+        *out = nullptr;
+        return ACCSPMM_SUCCESS;
+    }
+    uint32_t P = 1;
+    while (P < nb) P <<= 1;
+    OrderEntry e;
+    ACC_CUDA(cudaMalloc(&e.order, size_t(nb) * 4));
+    cudaError_t ce = cudaEventCreateWithFlags(&e.ready, cudaEventDisableTiming);
+    if (ce == cudaSuccess) {
+        block_order_kernel<<<1, 1024, size_t(P) * 8, s>>>(rwo, W, wb, nb, P, e.order);
+        ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess) ce = cudaEventRecord(e.ready, s);
+    if (ce != cudaSuccess) {
+        cudaStreamSynchronize(s);
+        cudaFree(e.order);
+        if (e.ready) cudaEventDestroy(e.ready);
+        ACC_FAIL(ACCSPMM_ERROR_CUDA, "block schedule: %s", cudaGetErrorString(ce));
+    }
+    g_order_cache.emplace(key, e);
+    *out = e.order;
+    return ACCSPMM_SUCCESS;
+}
+
 }  // namespace
+
+void schedule_cache_forget(const uint32_t* rwo) {
+    std::lock_guard<std::mutex> lock(g_order_mu);
+    for (auto it = g_order_cache.begin(); it != g_order_cache.end();) {
+        if (it->first.rwo == rwo) {
+            cudaFree(it->second.order);  // waits for queued work that reads it
+            cudaEventDestroy(it->second.ready);
+            it = g_order_cache.erase(it);
+        } else {
+            ++it;
+        }
+    }
+}
 
 int rwo_from_row_indices(const uint32_t* ri, uint32_t T, uint32_t W, uint32_t* rwo, uint32_t* err,
                          cudaStream_t s) {
@@ -401,16 +513,16 @@ uint32_t slice_width_for(uint32_t w_cfg, uint32_t T, uint32_t K, int precision) 
 int spmm_window_launch(const uint32_t* rwo, const uint32_t* tc_offset, const uint64_t* bits,
                        const uint32_t* a2b, const float* vals, uint32_t W, uint32_t w_cfg,
                        uint32_t T, uint32_t cols, const float* B, float* C, uint32_t K,
-                       int precision, cudaStream_t s) {
+                       int precision, cudaStream_t s, bool stable_rwo) {
     return spmm_window_launch_slices(rwo, tc_offset, bits, a2b, vals, W, w_cfg, T, cols, B, C, K,
-                                     precision, 0, 0xFFFFFFFFu, Epilogue{}, s, 0);
+                                     precision, 0, 0xFFFFFFFFu, Epilogue{}, s, 0, stable_rwo);
 }
 
 int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, const uint64_t* bits,
                               const uint32_t* a2b, const float* vals, uint32_t W, uint32_t w_cfg,
                               uint32_t T, uint32_t cols, const float* B, float* C, uint32_t K,
                               int precision, uint32_t slice_begin, uint32_t slice_count,
-                              const Epilogue& epi, cudaStream_t s, int slice_fs) {
+                              const Epilogue& epi, cudaStream_t s, int slice_fs, bool stable_rwo) {
     if (W == 0) return ACCSPMM_SUCCESS;
     // the launch shape depends only on (w_cfg, T, K, precision), so every
     // entry point cuts a matrix into the same pieces and sums partial windows
@@ -428,6 +540,18 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     slice_count = std::min(slice_count, slices - slice_begin);
     SpmmArgs a{rwo, tc_offset, bits, a2b, vals, B, C, W, cols, K, cfg.wb, slice_count,
                (W + cfg.wb - 1) / cfg.wb, cfg.slice_major, slice_begin, epi.bias, epi.act};
+    // A launch of a few waves ends with its heaviest window blocks: run them
+    // first (longest-processing-time order).  Larger launches keep window
+    // order, which keeps neighbouring windows' B rows in L2 together.  On the
+    // 16,384-row symmetric power-law matrix at K = 128 (683 blocks of 3
+    // windows, the heaviest 260 tiles against a mean of 95) the adaptive
+    // SpMM took 53.0 us instead of 62.0 us.
+    if (stable_rwo && !cfg.slice_major && a.n_wblocks <= kOrderMaxBlocks &&
+        uint64_t(a.n_wblocks) * a.n_slices <= uint64_t(kOrderMaxWaves) * sm_count() * uint32_t(cfg.occ) &&
+        env_int("ACCSPMM_SCHEDULE", 1) != 0) {
+        int st = cached_order(rwo, W, cfg.wb, a.n_wblocks, s, &a.order);
+        if (st) return st;
+    }
     // only the register-direct kernel has the epilogue; it cuts the matrix
     // into the same pieces as the other variants
     if (epi.bias || epi.act) cfg.kernel = kDirect;
@@ -472,7 +596,7 @@ int spmm_tf32_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t 
     if (st) return st;
     return spmm_window_launch(m->row_window_offset, m->tc_offset, m->tc_local_bit, m->sparse_a2b,
                               m->data, m->num_windows, m->num_windows, m->num_tiles, m->cols, B, C,
-                              K, precision, as_stream(stream));
+                              K, precision, as_stream(stream), m->owned != 0);
 }
 
 int spmm_bias_act_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K,
@@ -490,7 +614,7 @@ int spmm_bias_act_impl(const accspmm_metcf_t* m, const float* B, float* C, uint3
     return spmm_window_launch_slices(m->row_window_offset, m->tc_offset, m->tc_local_bit,
                                      m->sparse_a2b, m->data, m->num_windows, m->num_windows,
                                      m->num_tiles, m->cols, B, C, K, precision, 0, 0xFFFFFFFFu, epi,
-                                     as_stream(stream), 0);
+                                     as_stream(stream), 0, m->owned != 0);
 }
 
 namespace {
@@ -554,6 +678,7 @@ void adaptive_cache_forget(const accspmm_adpbme_t* ad) {
     std::lock_guard<std::mutex> lock(g_rwo_mu);
     for (auto it = g_rwo_cache.begin(); it != g_rwo_cache.end();) {
         if (it->first.ri == ad->row_indices) {
+            schedule_cache_forget(it->second.rwo);
             cudaFree(it->second.rwo);  // waits for queued work that reads it
             cudaEventDestroy(it->second.ready);
             it = g_rwo_cache.erase(it);
@@ -577,7 +702,7 @@ int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uin
         st = cached_rwo(ad, Weff, s, &rwo);
         if (st) return st;
         return spmm_window_launch(rwo, ad->tc_offset, ad->tc_local_bit, ad->sparse_a2b, ad->data, Weff,
-                                  (ad->rows + kWin - 1) / kWin, T, ad->cols, B, C, K, precision, s);
+                                  (ad->rows + kWin - 1) / kWin, T, ad->cols, B, C, K, precision, s, true);
     }
     // a caller-filled object may change between calls: derive every time
     DevBuf<uint32_t> scratch;  // rwo[Weff + 1] then an error word

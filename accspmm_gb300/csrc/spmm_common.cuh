@@ -30,6 +30,9 @@ struct SpmmArgs {
     uint32_t slice0;       // first feature slice of this launch
     const float* bias;     // epilogue: C = act(A B + bias[col]); nullptr: no bias
     uint32_t act;          // epilogue activation: 0 none, 1 ReLU
+    // CTA i runs window block order[i] (nullptr: block i).  Only the
+    // schedule changes: a block's arithmetic does not depend on its CTA.
+    const uint32_t* order = nullptr;
 };
 
 // TF32 operand rounded to nearest, ties away from zero: the reference's
@@ -245,6 +248,7 @@ struct Block {
             wbk = blockIdx.x / a.n_slices;
             slice = blockIdx.x - wbk * a.n_slices;
         }
+        if (a.order) wbk = __ldg(a.order + wbk);
         init_item(a, wbk, slice, s_rwo_mem, part_mem);
     }
 

@@ -212,7 +212,7 @@ int spmm_host_impl(const accspmm_metcf_t* m, const accspmm_adpbme_t* ad, const f
         HOST_CUDA(cudaStreamWaitEvent(s, in, 0));
         r = m ? spmm_window_launch_slices(rwo, m->tc_offset, m->tc_local_bit, m->sparse_a2b, m->data,
                                           W, w_cfg, T, cols, dBf, c_dev, K, precision, i, 1,
-                                          Epilogue{}, s, int(fs))
+                                          Epilogue{}, s, int(fs), m->owned != 0)
               : spmm_window_launch_slices(rwo, ad->tc_offset, ad->tc_local_bit, ad->sparse_a2b,
                                           ad->data, W, w_cfg, T, cols, dBf, c_dev, K, precision, i,
                                           1, Epilogue{}, s, int(fs));

@@ -309,3 +309,49 @@ def test_autotune_picks_a_shape_that_is_used_and_correct():
         np.testing.assert_array_equal(dCa.cpu().numpy()[:n], got[:n])
     finally:
         capi.load().accspmm_autotune_clear()
+
+
+def test_heaviest_first_schedule_keeps_results_bitwise(monkeypatch):
+    """Launches of a few waves run their window blocks heaviest first; the
+    schedule only changes which CTA runs a block, so plain and adaptive
+    results are bitwise equal with and without it."""
+    n, K = 16384, 128
+    r, c, v = synth.expand_symmetric(*synth.powerlaw_symmetric(n=n, seed=3))
+    csr = api.csr_from_coo(n, n, r, c, v)
+    m = device_metcf(csr)
+    a = m.adpbme()
+    cr = a.c_rows()
+    B = torch.rand((n, K), device="cuda") * 2 - 1
+    got = {}
+    for sched in ("1", "0"):
+        monkeypatch.setenv("ACCSPMM_SCHEDULE", sched)
+        C = empty_dev(m.c_rows, K)
+        Ca = empty_dev(cr, K)
+        m.spmm(B, C, K)
+        a.spmm(B, Ca, cr, K)
+        torch.cuda.synchronize()
+        got[sched] = (C, Ca)
+    assert torch.equal(got["1"][0], got["0"][0])
+    assert torch.equal(got["1"][1], got["0"][1])
+    assert torch.equal(got["1"][0][:n], got["1"][1][:n])
+    ref = oracle.spmm_csr_f64(csr["row_ptr"], csr["col_idx"], csr["data"], B.cpu().numpy())
+    assert rel_fro(got["1"][0][:n].cpu().numpy(), ref) < TOL_TF32_VS_F64
+
+
+def test_schedule_is_forgotten_with_its_matrix():
+    """A schedule is kept per library-owned matrix and dropped when the
+    matrix is destroyed: matrices built one after another (whose arrays may
+    reuse the freed addresses) each get their own."""
+    K = 64
+    for seed in range(4):
+        n = 4096 + 1024 * seed
+        r, c, v = synth.expand_symmetric(*synth.powerlaw_symmetric(n=n, seed=10 + seed))
+        csr = api.csr_from_coo(n, n, r, c, v)
+        m = device_metcf(csr)
+        B = np.random.default_rng(seed).uniform(-1, 1, (n, K)).astype(np.float32)
+        C = empty_dev(m.c_rows, K)
+        m.spmm(torch_dev(B), C, K)
+        torch.cuda.synchronize()
+        ref = oracle.spmm_csr_f64(csr["row_ptr"], csr["col_idx"], csr["data"], B)
+        assert rel_fro(C[:n].cpu().numpy(), ref) < TOL_TF32_VS_F64
+        m.destroy()
