@@ -13,9 +13,11 @@ is done between steps.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 --impl reference times the CPU CSR SpMM (the oracle's OpenMP port, the
-reference has no CPU SpMM of its own) on all host cores for the same metric.
-Under torchrun with more than one rank, every rank runs an independent replica
-on its own GPU (the workload does not shard in this build); rank 0 prints.
+reference has no CPU SpMM of its own) on all host cores for the same metric,
+and beside it the reference's own GPU kernels (compiled for sm_103a from its
+sources) on the same matrix.  Under torchrun with more than one rank, every
+rank runs an independent replica on its own GPU (row windows are independent,
+so replicas need no exchange); rank 0 prints.
 """
 from __future__ import annotations
 
