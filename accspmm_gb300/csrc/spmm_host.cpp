@@ -157,7 +157,10 @@ int spmm_host_impl(const accspmm_metcf_t* m, const accspmm_adpbme_t* ad, const f
 
     // C written by the kernel straight into host memory when it is pinned and
     // 16-byte aligned (the kernel stores float4s), else staged on the device
-    float* c_dev = (reinterpret_cast<uintptr_t>(C_host) & 15u) ? nullptr : mapped_host(C_host);
+    const char* direct_str = std::getenv("ACCSPMM_HOST_DIRECT");  // measurement override: 0 stages C
+    float* c_dev = (reinterpret_cast<uintptr_t>(C_host) & 15u) || (direct_str && std::atoi(direct_str) == 0)
+                       ? nullptr
+                       : mapped_host(C_host);
     const bool direct = c_dev != nullptr;
     if (direct_c) *direct_c = direct ? 1 : 0;
 
