@@ -528,6 +528,14 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     // entry point cuts a matrix into the same pieces and sums partial windows
     // in the same order
     Config cfg = choose_config(w_cfg, T, K, precision);
+    // The bias/activation epilogue lengthens the store path inside the tile
+    // loop; at 128-column slices that made the register-direct kernel spill
+    // (2.76 ms against 2.31 ms without the epilogue on the 1M-row matrix at
+    // K = 128), so epilogue launches use 64-column slices at 3 CTAs per SM,
+    // which keep the ring without spilling (2.56 ms, against 2.78 ms for the
+    // SpMM followed by a separate bias + ReLU pass).  Same blocks, same
+    // arithmetic.
+    if ((epi.bias || epi.act) && !slice_fs && cfg.fs == 128) slice_fs = 64;
     if (slice_fs && slice_fs != cfg.fs) {
         // another slice width (the feature columns a CTA covers do not change
         // any element's arithmetic; the window blocks stay the chooser's)

@@ -405,6 +405,14 @@ def run_ours(args):
         cr = a.c_rows(stream)
         Ca = torch.empty((cr, K), device=dev)
         a.spmm(B, Ca, cr, K, prec, stream)
+        # once each: the gather floor (a warm-up and one timed launch), the
+        # fused bias + ReLU epilogue, a row gather of B (the reordering path)
+        m.gather_floor(B, K, 1, stream)
+        bias = torch.rand((K,), device=dev, generator=gen)
+        m.spmm_bias_act(B, C, K, bias, capi.ACT_RELU, prec, stream)
+        perm = torch.randperm(n, device=dev, generator=gen).to(torch.int32)
+        PB = torch.empty_like(B)
+        api.permute_rows(B, PB, perm, n, K, False, stream)
         torch.cuda.synchronize()
         print(json.dumps({"profile_launches": args.profile, "K": K, "tiles": int(T)}))
         return
@@ -612,6 +620,13 @@ def run_small(args):
         else:
             m.spmm(B, C, K, prec, stream)
 
+    if args.profile:
+        # the command profiled by ncu: the block schedule and LAUNCHES steps
+        for _ in range(args.profile):
+            step()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_launches": args.profile, "K": K, "tiles": int(m.struct.num_tiles)}))
+        return
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
