@@ -87,3 +87,25 @@ def test_reordered_product_maps_back_to_the_original():
     torch.cuda.synchronize()
     ref = A.astype(np.float64) @ B.astype(np.float64)
     assert rel_fro(Cout.cpu().numpy(), ref) < TOL_TF32_VS_F64
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,K", [(1003, 12), (517, 260), (4, 128), (1, 4)])
+def test_row_permutation_is_exact(n, K):
+    """Gather and scatter move rows bit for bit, for row counts that are not
+    a multiple of the rows a warp moves and rows shorter and longer than one
+    warp's float4s."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(n + K)
+    perm = rng.permutation(n).astype(np.uint32)
+    B = rng.standard_normal((n, K)).astype(np.float32)
+    dB, dP = torch_dev(B), torch_dev(perm.view(np.int32))
+    G = torch.full((n, K), float("nan"), device="cuda")
+    S = torch.full((n, K), float("nan"), device="cuda")
+    api.permute_rows(dB, G, dP, n, K)
+    api.permute_rows(dB, S, dP, n, K, scatter=True)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(G.cpu().numpy(), B[perm])
+    want = np.empty_like(B)
+    want[perm] = B
+    np.testing.assert_array_equal(S.cpu().numpy(), want)
