@@ -682,6 +682,11 @@ int cached_rwo(const accspmm_adpbme_t* ad, uint32_t Weff, cudaStream_t s, const 
 
 }  // namespace
 
+int adaptive_rwo(const accspmm_adpbme_t* ad, uint32_t W, cudaStream_t s, const uint32_t** out) {
+    if (!ad->owned) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "only library-owned AdpBME objects are cached");
+    return cached_rwo(ad, W, s, out);
+}
+
 void adaptive_cache_forget(const accspmm_adpbme_t* ad) {
     std::lock_guard<std::mutex> lock(g_rwo_mu);
     for (auto it = g_rwo_cache.begin(); it != g_rwo_cache.end();) {

@@ -172,7 +172,11 @@ int spmm_host_impl(const accspmm_metcf_t* m, const accspmm_adpbme_t* ad, const f
         c_dev = static_cast<float*>(dC.p);
     }
     const uint32_t* rwo = m ? m->row_window_offset : nullptr;
-    if (ad) {
+    if (ad && ad->owned) {
+        // derived once per library-owned object and kept with it
+        r = adaptive_rwo(ad, W, s, &rwo);
+        if (r) return r;
+    } else if (ad) {
         // window offsets of the W real windows from rowIndices (windows past
         // W hold no tiles), the same derivation as accspmm_spmm_adaptive
         HOST_CUDA(cudaMallocFromPoolAsync(&dR.p, (size_t(W) + 2) * 4, ctx->pool, s));
@@ -218,7 +222,7 @@ int spmm_host_impl(const accspmm_metcf_t* m, const accspmm_adpbme_t* ad, const f
                                           Epilogue{}, s, int(fs), m->owned != 0)
               : spmm_window_launch_slices(rwo, ad->tc_offset, ad->tc_local_bit, ad->sparse_a2b,
                                           ad->data, W, w_cfg, T, cols, dBf, c_dev, K, precision, i,
-                                          1, Epilogue{}, s, int(fs));
+                                          1, Epilogue{}, s, int(fs), ad->owned != 0);
         if (r) return r;
         if (!direct) {
             cudaEvent_t done;

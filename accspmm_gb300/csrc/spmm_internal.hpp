@@ -73,6 +73,9 @@ int spmm_tf32_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t 
                    void* stream);
 // Drops the window offsets cached for an owned AdpBME (before its arrays are freed).
 void adaptive_cache_forget(const accspmm_adpbme_t* ad);
+// Window offsets of W windows derived from an owned AdpBME's rowIndices, kept
+// with the object until accspmm_adpbme_destroy.
+int adaptive_rwo(const accspmm_adpbme_t* ad, uint32_t W, cudaStream_t s, const uint32_t** out);
 int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uint32_t c_rows,
                        uint32_t K, int precision, void* stream);
 int device_status_impl(void* stream);
