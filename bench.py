@@ -89,6 +89,12 @@ def workload(n: int, seed: int):
     return rp, ci, v
 
 
+def degree_stats(rp):
+    """Realised row degrees of a CSR matrix (the generators state targets)."""
+    d = np.diff(np.asarray(rp, dtype=np.int64))
+    return {"mean": round(float(d.mean()), 2), "max": int(d.max()), "min": int(d.min())}
+
+
 def workload_name(n, k):
     return (f"powerlaw_local N={n} mean_deg=32 zipf=2.1 max_deg=4096 local=50%/+-1024 "
             f"B=N x {k} fp32 uniform[-1,1)")
@@ -309,6 +315,7 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
         "data": "synthetic", "impl": "reference",
         "config": {"workload": wname, "n_rows": args.n, "nnz": int(len(ci)),
+                   "realised_degree": degree_stats(rp),
                    "K": args.k, "path": "CPU CSR SpMM (oracle port; the reference has no CPU SpMM)"},
         "cpu_baseline": {"value": round(gf, 2), "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{rows_per_step} consecutive rows per step (of {args.n}), "
@@ -566,6 +573,7 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": args.precision, "data": "synthetic",
         "config": {"workload": workload_name(n, K), "n_rows": n, "nnz": nnz, "K": K,
+                   "realised_degree": degree_stats(rp),
                    "tiles": int(T), "windows": int(W), "groups": G,
                    "path": "adaptive" if adaptive else "plain",
                    "parallelism": "replicas" if world > 1 else "single GPU",
@@ -663,6 +671,7 @@ def run_small(args):
         "dtype": args.precision, "data": "synthetic",
         "config": {"workload": small_workload_name(K),
                    "n_rows": n, "nnz": nnz, "K": K, "tiles": int(T), "windows": int(W), "groups": G,
+                   "realised_degree": degree_stats(csr["row_ptr"]),
                    "path": "adaptive" if adaptive else "plain",
                    "l2": "flushed before every timed step (256 MB written)"},
         "no_flush": {"ms_per_step": round(warm_ms, 5),
