@@ -256,8 +256,11 @@ __global__ void __launch_bounds__(1024) block_order_kernel(const uint32_t* __res
 }
 
 // Heaviest-first schedules of library-owned matrices, per (window offsets,
-// windows, windows per block, device); computed on the calling stream the
-// first time, later calls on other streams wait for that computation.
+// windows, windows per block, device).  The first call computes one on its
+// stream and waits for it on the host, so every kept schedule is complete:
+// later calls on any stream, including calls captured into a CUDA graph, use
+// it without an event wait (a capturing stream may not wait on an event
+// recorded outside the capture).
 struct OrderKey {
     const uint32_t* rwo;
     uint32_t W, wb;
@@ -268,7 +271,6 @@ struct OrderKey {
 };
 struct OrderEntry {
     uint32_t* order = nullptr;
-    cudaEvent_t ready = nullptr;
 };
 std::mutex g_order_mu;
 std::map<OrderKey, OrderEntry> g_order_cache;
@@ -281,7 +283,6 @@ int cached_order(const uint32_t* rwo, uint32_t W, uint32_t wb, uint32_t nb, cuda
     std::lock_guard<std::mutex> lock(g_order_mu);
     auto it = g_order_cache.find(key);
     if (it != g_order_cache.end()) {
-        ACC_CUDA(cudaStreamWaitEvent(s, it->second.ready, 0));
         *out = it->second.order;
         return ACCSPMM_SUCCESS;
     }
@@ -298,16 +299,12 @@ int cached_order(const uint32_t* rwo, uint32_t W, uint32_t wb, uint32_t nb, cuda
     while (P < nb) P <<= 1;
     OrderEntry e;
     ACC_CUDA(cudaMalloc(&e.order, size_t(nb) * 4));
-    cudaError_t ce = cudaEventCreateWithFlags(&e.ready, cudaEventDisableTiming);
-    if (ce == cudaSuccess) {
-        block_order_kernel<<<1, 1024, size_t(P) * 8, s>>>(rwo, W, wb, nb, P, e.order);
-        ce = cudaGetLastError();
-    }
-    if (ce == cudaSuccess) ce = cudaEventRecord(e.ready, s);
+    block_order_kernel<<<1, 1024, size_t(P) * 8, s>>>(rwo, W, wb, nb, P, e.order);
+    cudaError_t ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
     if (ce != cudaSuccess) {
         cudaStreamSynchronize(s);
         cudaFree(e.order);
-        if (e.ready) cudaEventDestroy(e.ready);
         ACC_FAIL(ACCSPMM_ERROR_CUDA, "block schedule: %s", cudaGetErrorString(ce));
     }
     g_order_cache.emplace(key, e);
@@ -322,7 +319,6 @@ void schedule_cache_forget(const uint32_t* rwo) {
     for (auto it = g_order_cache.begin(); it != g_order_cache.end();) {
         if (it->first.rwo == rwo) {
             cudaFree(it->second.order);  // waits for queued work that reads it
-            cudaEventDestroy(it->second.ready);
             it = g_order_cache.erase(it);
         } else {
             ++it;
@@ -631,6 +627,9 @@ namespace {
 // kept per (rowIndices array, window count, device) so that repeated adaptive
 // calls on one object derive them once.  Library-owned arrays are not changed
 // after they are built; accspmm_adpbme_destroy forgets the object's entries.
+// The first call derives them on its stream and waits for that on the host,
+// so kept offsets are complete and later calls on any stream, or captured
+// into a CUDA graph, use them without an event wait.
 struct RwoKey {
     const uint32_t* ri;
     uint32_t weff;
@@ -639,13 +638,12 @@ struct RwoKey {
 };
 struct RwoEntry {
     uint32_t* rwo = nullptr;  // [weff + 2]: offsets, then an error word
-    cudaEvent_t ready = nullptr;
 };
 std::mutex g_rwo_mu;
 std::map<RwoKey, RwoEntry> g_rwo_cache;
 
-// Cached offsets of an owned AdpBME (computed on `s` the first time; later
-// calls on other streams wait for that computation).
+// Cached offsets of an owned AdpBME (computed on `s`, and waited for, the
+// first time).
 int cached_rwo(const accspmm_adpbme_t* ad, uint32_t Weff, cudaStream_t s, const uint32_t** out) {
     int dev = 0;
     ACC_CUDA(cudaGetDevice(&dev));
@@ -653,28 +651,27 @@ int cached_rwo(const accspmm_adpbme_t* ad, uint32_t Weff, cudaStream_t s, const 
     std::lock_guard<std::mutex> lock(g_rwo_mu);
     auto it = g_rwo_cache.find(key);
     if (it == g_rwo_cache.end()) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        ACC_CUDA(cudaStreamIsCapturing(s, &cs));
+        if (cs != cudaStreamCaptureStatusNone)
+            ACC_FAIL(ACCSPMM_ERROR_UNSUPPORTED,
+                     "the first adaptive call on an AdpBME derives its window offsets and must not be "
+                     "captured into a graph: call it once outside the capture");
         RwoEntry e;
         ACC_CUDA(cudaMalloc(&e.rwo, (size_t(Weff) + 2) * 4));
-        cudaError_t ce = cudaEventCreateWithFlags(&e.ready, cudaEventDisableTiming);
-        if (ce == cudaSuccess) ce = cudaMemsetAsync(e.rwo + Weff + 1, 0, 4, s);
-        if (ce != cudaSuccess) {
-            cudaFree(e.rwo);
-            if (e.ready) cudaEventDestroy(e.ready);
-            ACC_FAIL(ACCSPMM_ERROR_CUDA, "window-offset cache: %s", cudaGetErrorString(ce));
+        cudaError_t ce = cudaMemsetAsync(e.rwo + Weff + 1, 0, 4, s);
+        if (ce == cudaSuccess) {
+            rwo_from_row_indices_kernel<<<(Weff + 1 + 255) / 256, 256, 0, s>>>(
+                ad->row_indices, ad->num_tiles, Weff, e.rwo, e.rwo + Weff + 1);
+            ce = cudaGetLastError();
         }
-        rwo_from_row_indices_kernel<<<(Weff + 1 + 255) / 256, 256, 0, s>>>(ad->row_indices, ad->num_tiles,
-                                                                           Weff, e.rwo, e.rwo + Weff + 1);
-        ce = cudaGetLastError();
-        if (ce == cudaSuccess) ce = cudaEventRecord(e.ready, s);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
         if (ce != cudaSuccess) {
             cudaStreamSynchronize(s);
             cudaFree(e.rwo);
-            cudaEventDestroy(e.ready);
             ACC_FAIL(ACCSPMM_ERROR_CUDA, "window-offset cache: %s", cudaGetErrorString(ce));
         }
         it = g_rwo_cache.emplace(key, e).first;
-    } else {
-        ACC_CUDA(cudaStreamWaitEvent(s, it->second.ready, 0));
     }
     *out = it->second.rwo;
     return ACCSPMM_SUCCESS;
@@ -693,7 +690,6 @@ void adaptive_cache_forget(const accspmm_adpbme_t* ad) {
         if (it->first.ri == ad->row_indices) {
             schedule_cache_forget(it->second.rwo);
             cudaFree(it->second.rwo);  // waits for queued work that reads it
-            cudaEventDestroy(it->second.ready);
             it = g_rwo_cache.erase(it);
         } else {
             ++it;

@@ -237,7 +237,13 @@ void accspmm_adpbme_destroy(accspmm_adpbme_t* adp);
 /* TF32Compute::compute, include/tf32_comp.hpp:52-80 (kernels
  * tf32_mma_kernel / tf32_mma_g512_kernel, include/mma_tf32.cuh:13-550), one
  * launch, no timing loop.  C = decode(METCF) * B over all 8W rows; C is
- * fully written (rows of empty windows become 0).  Device METCF, B, C. */
+ * fully written (rows of empty windows become 0).  Device METCF, B, C.
+ * Launches of a few waves of a library-owned METCF run their window blocks
+ * heaviest first: the first such call per (matrix, window block size) sorts
+ * the blocks on the GPU, waits for that on the host once, and keeps the
+ * schedule until accspmm_metcf_destroy (results do not depend on it).
+ * Calls may be captured into a CUDA graph; a call captured before the
+ * schedule exists runs the blocks in window order. */
 int accspmm_spmm_tf32(const accspmm_metcf_t* metcf, const float* B, float* C,
                       uint32_t K, int32_t precision, void* stream);
 
@@ -249,8 +255,11 @@ int accspmm_spmm_tf32(const accspmm_metcf_t* metcf, const float* B, float* C,
  * overwritten, where the reference accumulated into a pre-zeroed C.  The
  * window offsets derived from rowIndices (4 (c_rows/8 + 2) bytes) are kept
  * with a library-owned AdpBME after its first call, until
- * accspmm_adpbme_destroy; for an AdpBME the caller filled they are derived
- * into stream-ordered scratch on every call. */
+ * accspmm_adpbme_destroy: that first call per (object, c_rows) derives them
+ * and waits for them on the host once, and must not be captured into a CUDA
+ * graph (it returns ACCSPMM_ERROR_UNSUPPORTED inside a capture); later calls
+ * may be captured.  For an AdpBME the caller filled they are derived into
+ * stream-ordered scratch on every call. */
 int accspmm_spmm_adaptive(const accspmm_adpbme_t* adp, const float* B,
                           float* C, uint32_t c_rows, uint32_t K,
                           int32_t precision, void* stream);

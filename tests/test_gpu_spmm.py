@@ -355,3 +355,49 @@ def test_schedule_is_forgotten_with_its_matrix():
         ref = oracle.spmm_csr_f64(csr["row_ptr"], csr["col_idx"], csr["data"], B)
         assert rel_fro(C[:n].cpu().numpy(), ref) < TOL_TF32_VS_F64
         m.destroy()
+
+
+def test_spmm_calls_capture_into_a_cuda_graph():
+    """After one call outside a capture (which derives and keeps the adaptive
+    window offsets and the block schedule), the plain, adaptive and epilogue
+    entry points can be captured into a CUDA graph; replays with new B
+    contents give bitwise the results of direct calls.  A first adaptive call
+    inside a capture is refused with a status, not run."""
+    n, K = 16384, 128
+    r, c, v = synth.expand_symmetric(*synth.powerlaw_symmetric(n=n, seed=5))
+    csr = api.csr_from_coo(n, n, r, c, v)
+    m = device_metcf(csr)
+    a = m.adpbme()
+    cr = a.c_rows()
+    B = torch.rand((n, K), device="cuda") * 2 - 1
+    bias = torch.rand((K,), device="cuda")
+    C, Ca, Ce = empty_dev(m.c_rows, K), empty_dev(cr, K), empty_dev(m.c_rows, K)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        m.spmm(B, C, K, stream=s)  # outside any capture: builds the cached state
+        a.spmm(B, Ca, cr, K, stream=s)
+        m.spmm_bias_act(B, Ce, K, bias, capi.ACT_RELU, stream=s)
+    s.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        st = torch.cuda.current_stream()
+        m.spmm(B, C, K, stream=st)
+        a.spmm(B, Ca, cr, K, stream=st)
+        m.spmm_bias_act(B, Ce, K, bias, capi.ACT_RELU, stream=st)
+    for seed in range(2):
+        B.copy_(torch.rand((n, K), device="cuda", generator=torch.Generator("cuda").manual_seed(seed)) * 2 - 1)
+        g.replay()
+        torch.cuda.synchronize()
+        D, Da, De = empty_dev(m.c_rows, K), empty_dev(cr, K), empty_dev(m.c_rows, K)
+        m.spmm(B, D, K)
+        a.spmm(B, Da, cr, K)
+        m.spmm_bias_act(B, De, K, bias, capi.ACT_RELU)
+        torch.cuda.synchronize()
+        assert torch.equal(C, D) and torch.equal(Ca, Da) and torch.equal(Ce, De)
+    a2 = m.adpbme()
+    C2 = empty_dev(cr, K)
+    g2 = torch.cuda.CUDAGraph()
+    with pytest.raises(capi.AccSpmmError):
+        with torch.cuda.graph(g2, stream=s):
+            a2.spmm(B, C2, cr, K, stream=torch.cuda.current_stream())
+    torch.cuda.synchronize()
