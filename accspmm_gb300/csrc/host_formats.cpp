@@ -1,12 +1,20 @@
 // host_formats.cpp -- host side of the path: Matrix Market reader, COO -> CSR,
 // CSR -> METCF, METCF -> AdpBME, balance strategy.  All multi-threaded over
 // the host cores; results are independent of the thread count.
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <algorithm>
 #include <cerrno>
 #include <cstdarg>
 #include <cstdlib>
+#include <charconv>
 #include <cstring>
+#include <memory>
 #include <numeric>
+#include <string>
 
 #include "common.hpp"
 #include "host_formats.hpp"
@@ -112,19 +120,43 @@ const char* line_end(const char* p, const char* e) {
 
 }  // namespace
 
+// The file's bytes, mapped read-only (the parsing threads fault its pages in
+// in parallel; no copy).  Every parse below is bounded by explicit ends, so
+// no terminating NUL is needed.
+struct MappedFile {
+    const char* p = nullptr;
+    size_t n = 0;
+    ~MappedFile() {
+        if (p && n) munmap(const_cast<char*>(p), n);
+    }
+};
+
 int read_mtx_host(const char* path, accspmm_coo_t* coo) {
     std::memset(coo, 0, sizeof *coo);
-    FILE* f = std::fopen(path, "rb");
-    if (!f) ACC_FAIL(ACCSPMM_MM_LOADING_FILE_ERROR, "cannot open %s: %s", path, std::strerror(errno));
-    std::fseek(f, 0, SEEK_END);
-    long sz = std::ftell(f);
-    std::fseek(f, 0, SEEK_SET);
-    std::vector<char> buf(size_t(sz > 0 ? sz : 0) + 1);
-    size_t got = sz > 0 ? std::fread(buf.data(), 1, size_t(sz), f) : 0;
-    std::fclose(f);
-    buf[got] = '\0';
-    const char* p = buf.data();
-    const char* e = p + got;
+    MappedFile mf;
+    {
+        const int fd = open(path, O_RDONLY);
+        if (fd < 0) ACC_FAIL(ACCSPMM_MM_LOADING_FILE_ERROR, "cannot open %s: %s", path, std::strerror(errno));
+        struct stat sb;
+        if (fstat(fd, &sb) != 0) {
+            close(fd);
+            ACC_FAIL(ACCSPMM_MM_LOADING_FILE_ERROR, "cannot stat %s: %s", path, std::strerror(errno));
+        }
+        mf.n = size_t(sb.st_size);
+        if (mf.n) {
+            void* m = mmap(nullptr, mf.n, PROT_READ, MAP_PRIVATE, fd, 0);
+            if (m == MAP_FAILED) {
+                close(fd);
+                mf.n = 0;
+                ACC_FAIL(ACCSPMM_MM_LOADING_FILE_ERROR, "cannot map %s: %s", path, std::strerror(errno));
+            }
+            mf.p = static_cast<const char*>(m);
+        }
+        close(fd);
+    }
+    static const char kEmpty[1] = {0};
+    const char* p = mf.n ? mf.p : kEmpty;
+    const char* e = p + mf.n;
 
     // banner: first line (fgets of at most 1024 chars, mmio.hpp:35)
     const char* le = line_end(p, e);
@@ -200,9 +232,19 @@ int read_mtx_host(const char* path, accspmm_coo_t* coo) {
         ACC_FAIL(ACCSPMM_ERROR_READ_MTX, "%s: %u entries announced, file ends early", path, nz);
 
     // raw 1-based indices and values; an entry may straddle two chunks, so
-    // each token is stored where it belongs and validated in a second pass
-    std::vector<uint32_t> tr(nz), tc(nz);
-    std::vector<float> tv(nz, 1.0f);  // pattern entries are 1.0, mmio.hpp:127
+    // each token is stored where it belongs and validated in a second pass.
+    // Without a symmetric expansion they are parsed straight into the COO.
+    struct Free {
+        void operator()(void* q) const { std::free(q); }
+    };
+    std::unique_ptr<uint32_t, Free> ur(host_alloc<uint32_t>(nz)), uc(host_alloc<uint32_t>(nz));
+    std::unique_ptr<float, Free> uv(host_alloc<float>(nz));
+    if (!ur || !uc || !uv) ACC_FAIL(ACCSPMM_ERROR_ALLOC, "host allocation failed");
+    uint32_t* tr = ur.get();
+    uint32_t* tc = uc.get();
+    float* tv = uv.get();
+    if (tpe == 2)  // pattern entries are 1.0, mmio.hpp:127
+        parallel_chunks(nz, [&](size_t b, size_t en, unsigned) { std::fill(tv + b, tv + en, 1.0f); });
     std::vector<int> bad(nch, 0);
     parallel_chunks(nch, [&](size_t b, size_t en, unsigned) {
         for (size_t c = b; c < en; ++c) {
@@ -222,9 +264,20 @@ int read_mtx_host(const char* path, accspmm_coo_t* coo) {
                     if (!parse_u32(z, q, &v) || z != q) { bad[c] = 1; break; }
                     (field == 0 ? tr : tc)[entry] = v;
                 } else if (field == 2) {
-                    char* z = nullptr;
-                    double v = std::strtod(tokb, &z);
-                    if (z != q) { bad[c] = 1; break; }
+                    // std::from_chars: correctly rounded like strtod, without
+                    // the locale; it takes no '+', which fscanf("%lf") does
+                    const char* tb = tokb;
+                    if (*tb == '+' && q - tb > 1 && tb[1] != '+' && tb[1] != '-') ++tb;
+                    double v = 0.0;
+                    const auto fc = std::from_chars(tb, q, v);
+                    if (fc.ec != std::errc() || fc.ptr != q) {
+                        // hexadecimal floats and out-of-range values: the C
+                        // library's parse, on a NUL-terminated copy
+                        std::string tok(tokb, q);
+                        char* z = nullptr;
+                        v = std::strtod(tok.c_str(), &z);
+                        if (z != tok.c_str() + tok.size()) { bad[c] = 1; break; }
+                    }
                     tv[entry] = float(v);
                 }
                 // field 3 is the imaginary part, dropped (mmio.hpp:123)
@@ -281,12 +334,9 @@ int read_mtx_host(const char* path, accspmm_coo_t* coo) {
         });
     } else {
         coo->nnz = nz;
-        coo->row = host_alloc<uint32_t>(nz);
-        coo->col = host_alloc<uint32_t>(nz);
-        coo->data = host_alloc<float>(nz);
-        std::memcpy(coo->row, tr.data(), sizeof(uint32_t) * nz);
-        std::memcpy(coo->col, tc.data(), sizeof(uint32_t) * nz);
-        std::memcpy(coo->data, tv.data(), sizeof(float) * nz);
+        coo->row = ur.release();
+        coo->col = uc.release();
+        coo->data = uv.release();
     }
     return ACCSPMM_SUCCESS;
 }
