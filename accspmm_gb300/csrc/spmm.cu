@@ -543,7 +543,7 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     if (slice_begin >= slices) return ACCSPMM_SUCCESS;
     slice_count = std::min(slice_count, slices - slice_begin);
     SpmmArgs a{rwo, tc_offset, bits, a2b, vals, B, C, W, cols, K, cfg.wb, slice_count,
-               (W + cfg.wb - 1) / cfg.wb, cfg.slice_major, slice_begin, epi.bias, epi.act};
+               (W + cfg.wb - 1) / cfg.wb, cfg.slice_major, slice_begin, epi.bias, epi.act, nullptr};
     // A launch of a few waves ends with its heaviest window blocks: run them
     // first (longest-processing-time order).  Larger launches keep window
     // order, which keeps neighbouring windows' B rows in L2 together.  On the

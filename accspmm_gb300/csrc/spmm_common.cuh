@@ -32,7 +32,9 @@ struct SpmmArgs {
     uint32_t act;          // epilogue activation: 0 none, 1 ReLU
     // CTA i runs window block order[i] (nullptr: block i).  Only the
     // schedule changes: a block's arithmetic does not depend on its CTA.
-    const uint32_t* order = nullptr;
+    // (No default member initializer: the batched kernel keeps a SpmmArgs in
+    // shared memory; brace initialisation without it leaves it null.)
+    const uint32_t* order;
 };
 
 // TF32 operand rounded to nearest, ties away from zero: the reference's
