@@ -299,8 +299,10 @@ int accspmm_spmm_chain(const accspmm_metcf_t* metcf, const float* B, float* C,
  * (plain path) and `adp` (adaptive path), on the device.  B_host has `cols`
  * rows and K columns; C_host receives A * B as 8 * ceil(rows / 8) rows of K
  * columns (both paths; the adaptive path's extra zero rows are not written).
- * The work is cut into the feature slices of the device entry points, and
- * the host-to-device copy of slice i + 1 overlaps the kernel of slice i.
+ * The work is cut into feature slices of about a quarter of K (32 to 64
+ * columns), and the host-to-device copy of slice i + 1 overlaps the kernel
+ * of slice i.  For a library-owned AdpBME the first call derives and keeps
+ * its window offsets (one host wait), as accspmm_spmm_adaptive does.
  * When C_host is page-locked (cudaHostAlloc / cudaHostRegister) and 16-byte
  * aligned the kernel writes C straight into it over the host link;
  * otherwise C is staged on the device and copied back slice by slice.
