@@ -68,3 +68,11 @@ def test_reference_arm_gpu_kernels():
     assert g["by_k"]["64"]["ms"] > 0
     assert g["path"] == "plain" or g["plain_kernel_by_k"]["64"]["ms"] > 0
     assert d["value"] > 0 and d["impl"] == "reference"
+
+
+def test_profile_modes_run():
+    """The commands the ncu summaries were made with keep running."""
+    d = run("--profile", "1", "--n", "65536", "--k", "64")
+    assert d["profile_launches"] == 1 and d["tiles"] > 0
+    d = run("--workload", "small", "--profile", "2")
+    assert d["profile_launches"] == 2
