@@ -865,7 +865,7 @@ def run_serve(args):
     rng = np.random.default_rng(args.seed)
     n_graphs = 64
     row_hi = args.rows_hi or 500000
-    graphs = []
+    graphs, csrs = [], []
     for i in range(n_graphs):
         rows = int(np.exp(rng.uniform(np.log(2000), np.log(row_hi))))
         deg = synth.powerlaw_degrees(rows, 2.1, 16.0, min(rows, 4096), rng)
@@ -876,6 +876,7 @@ def run_serve(args):
         rp, ci, vals = synth.coo_to_csr(rows, r, c, v)
         csr = dict(rows=rows, cols=rows, nnz=len(ci), row_ptr=rp, col_idx=ci, data=vals)
         graphs.append(api.DeviceMETCF.from_csr(api.DeviceCSR.upload(csr)))
+        csrs.append((rp, ci, vals))
     torch.cuda.synchronize()
     ks = [32, 64, 128, 256, 512]
     max_rows = max(g.c_rows for g in graphs)
@@ -969,6 +970,31 @@ def run_serve(args):
                               "mean_batch": round(st["mean_batch"], 2), "launches": st["launches"]}
         srv.destroy()
         results[name] = out
+    # the stated error: served results (single products and A (A B) chains)
+    # against FP64 products of the same graphs and B (torch's sparse CSR
+    # matmul in float64 on the GPU)
+    srv = api.Server(graphs, budget, max_batch=64, streams=4)
+    erng = np.random.default_rng(args.seed + 1)
+    errs = []
+    for j in range(8):
+        g, k = int(erng.integers(0, n_graphs)), int(erng.choice(ks))
+        hops = 2 if j % 4 == 3 else 1
+        nr = len(csrs[g][0]) - 1
+        Cbuf = torch.empty((graphs[g].c_rows * k,), dtype=torch.float32, pin_memory=True)
+        rid = srv.submit(g, Bh, Cbuf, k, prec, hops)
+        assert srv.wait(rid, 120000) == 0
+        rp, ci, vals = csrs[g]
+        A = torch.sparse_csr_tensor(torch.from_numpy(rp.astype(np.int64)), torch.from_numpy(ci.astype(np.int64)),
+                                    torch.from_numpy(vals.astype(np.float64)), size=(nr, nr), device="cuda")
+        ref = A @ Bh[:nr * k].view(nr, k).to("cuda", torch.float64)
+        if hops == 2:
+            ref = A @ ref
+        got = Cbuf.view(-1, k)[:nr].to("cuda", torch.float64)
+        errs.append(float((got - ref).norm() / ref.norm()))
+    srv.destroy()
+    served_error = {"rel_fro_vs_fp64_max": max(errs), "rel_fro_vs_fp64_median": float(np.median(errs)),
+                    "samples": len(errs), "two_layer_chains": 2,
+                    "reference": "torch sparse CSR matmul in float64 on the GPU"}
     best = max(v["achieved_rps"] for v in results["continuous_batching"].values())
     base = max(v["achieved_rps"] for v in results["per_request"].values())
     out = {
@@ -986,6 +1012,7 @@ def run_serve(args):
                    "graph_nnz": int(sum(g.struct.nnz for g in graphs))},
         "serve": results,
         "per_request_best_rps": base,
+        "served_error": served_error,
     }
     print(json.dumps(out))
 

@@ -49,6 +49,7 @@ def test_serve_mode_small():
     d = run("--workload", "serve", "--rows-hi", "8000", timeout=900)
     cb = d["serve"]["continuous_batching"]
     assert all(v["achieved_rps"] > 0 and v["p99_ms"] >= v["p50_ms"] for v in cb.values())
+    assert d["served_error"]["rel_fro_vs_fp64_max"] < 1e-3  # the TF32 tolerance
 
 
 def test_small_mode():
