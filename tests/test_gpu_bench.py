@@ -37,6 +37,7 @@ def test_batch_mode_small():
     d = run("--workload", "batch", "--graphs", "12", "--rows-hi", "5000", "--steps", "2",
             "--warmup", "3")
     assert d["batch"]["bitwise_equal_to_separate"] is True
+    assert d["batch"]["rel_fro_vs_fp64_max"] < 1e-3
     assert d["config"]["graphs"] == 12 and d["value"] > 0
 
 
