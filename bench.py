@@ -467,6 +467,20 @@ def run_ours(args):
     flops = 2.0 * nnz * K
     ms, value = replica_throughput(ms, flops, world, dev)
 
+    def fp64_error(C_out, Bt):
+        """Relative Frobenius error of a product against the FP64 product
+        (torch's sparse CSR matmul in float64 on the GPU)."""
+        A = torch.sparse_csr_tensor(torch.from_numpy(rp.astype(np.int64)), torch.from_numpy(ci.astype(np.int64)),
+                                    torch.from_numpy(vals.astype(np.float64)), size=(n, n), device=dev)
+        want = A @ Bt.double()
+        err = float((C_out[:n].double() - want).norm() / want.norm())
+        del A, want
+        return err
+
+    # the error of the timed step's product (C holds the last step's result)
+    accuracy = {"rel_fro_vs_fp64": fp64_error(C, B),
+                "reference": "torch sparse CSR matmul in float64 on the GPU"}
+
     # dominant kernel alone: the plain entry point is exactly one launch of it
     for _ in range(3):
         m.spmm(B, C, K, prec, stream)
@@ -585,6 +599,7 @@ def run_ours(args):
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "accuracy": accuracy,
         "gpu_launches": args.steps * launches_per_step,
         "clocks": clk.summary(),
         "k_sweep": sweep,

@@ -31,6 +31,7 @@ def test_scale_mode_small():
     assert d["roofline"]["bound"] == "hbm" and 0 < d["roofline"]["frac"]
     assert d["e2e"]["h2d_bytes_per_step"] == 65536 * 64 * 4
     assert d["roofline"]["gather_model"]["floor_ms"] > 0
+    assert d["accuracy"]["rel_fro_vs_fp64"] < 1e-3
 
 
 def test_batch_mode_small():
