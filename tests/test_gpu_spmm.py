@@ -401,3 +401,31 @@ def test_spmm_calls_capture_into_a_cuda_graph():
         with torch.cuda.graph(g2, stream=s):
             a2.spmm(B, C2, cr, K, stream=torch.cuda.current_stream())
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("kernel", ["pipe", "bulk", "tma", "lean", "db"])
+@pytest.mark.parametrize("name,K", [("plsym1000", 32), ("plsym1000", 128), ("longwin", 64)])
+def test_measurement_kernel_variants(monkeypatch, kernel, name, K):
+    """The kernel variants kept for measurement (ACCSPMM_KERNEL) compute the
+    same product: bitwise equal to the default register-direct kernel where
+    they cut the window blocks among the same 8 warps (lean, db), within the
+    TF32 emulation tolerance where they use 4 warps per CTA (pipe, bulk,
+    tma: their warps' pieces, and so the partial-window sums, differ)."""
+    g = gold(name)
+    csr = csr_of_gold(g)
+    m = device_metcf(csr)
+    h = m.to_numpy()
+    B = np.random.default_rng(K).uniform(-1, 1, (csr["cols"], K)).astype(np.float32)
+    dB = torch_dev(B)
+    C0 = empty_dev(m.c_rows, K)
+    m.spmm(dB, C0, K)
+    monkeypatch.setenv("ACCSPMM_KERNEL", kernel)
+    C1 = empty_dev(m.c_rows, K)
+    m.spmm(dB, C1, K)
+    torch.cuda.synchronize()
+    capi.call("accspmm_device_status", None)  # raises if a bounded wait expired
+    if kernel in ("lean", "db"):
+        assert torch.equal(C0, C1)
+    got = C1.cpu().numpy()
+    assert rel_fro(got, oracle.spmm_metcf_tf32(h, csr["cols"], B)) < TOL_TF32_VS_EMU
+    assert rel_fro(got, oracle.spmm_metcf_f64(h, csr["cols"], B)) < TOL_TF32_VS_F64
