@@ -403,9 +403,10 @@ def test_spmm_calls_capture_into_a_cuda_graph():
     torch.cuda.synchronize()
 
 
+@pytest.mark.parametrize("prec", [capi.PREC_TF32, capi.PREC_3XTF32])
 @pytest.mark.parametrize("kernel", ["pipe", "bulk", "tma", "lean", "db"])
 @pytest.mark.parametrize("name,K", [("plsym1000", 32), ("plsym1000", 128), ("longwin", 64)])
-def test_measurement_kernel_variants(monkeypatch, kernel, name, K):
+def test_measurement_kernel_variants(monkeypatch, kernel, name, K, prec):
     """The kernel variants kept for measurement (ACCSPMM_KERNEL) compute the
     same product: bitwise equal to the default register-direct kernel where
     they cut the window blocks among the same 8 warps (lean, db), within the
@@ -418,14 +419,18 @@ def test_measurement_kernel_variants(monkeypatch, kernel, name, K):
     B = np.random.default_rng(K).uniform(-1, 1, (csr["cols"], K)).astype(np.float32)
     dB = torch_dev(B)
     C0 = empty_dev(m.c_rows, K)
-    m.spmm(dB, C0, K)
+    m.spmm(dB, C0, K, prec)
     monkeypatch.setenv("ACCSPMM_KERNEL", kernel)
     C1 = empty_dev(m.c_rows, K)
-    m.spmm(dB, C1, K)
+    m.spmm(dB, C1, K, prec)
     torch.cuda.synchronize()
     capi.call("accspmm_device_status", None)  # raises if a bounded wait expired
     if kernel in ("lean", "db"):
         assert torch.equal(C0, C1)
     got = C1.cpu().numpy()
-    assert rel_fro(got, oracle.spmm_metcf_tf32(h, csr["cols"], B)) < TOL_TF32_VS_EMU
-    assert rel_fro(got, oracle.spmm_metcf_f64(h, csr["cols"], B)) < TOL_TF32_VS_F64
+    f64 = oracle.spmm_metcf_f64(h, csr["cols"], B)
+    if prec == capi.PREC_TF32:
+        assert rel_fro(got, oracle.spmm_metcf_tf32(h, csr["cols"], B)) < TOL_TF32_VS_EMU
+        assert rel_fro(got, f64) < TOL_TF32_VS_F64
+    else:
+        assert rel_fro(got, f64) < TOL_3XTF32_VS_F64
