@@ -434,3 +434,48 @@ def test_measurement_kernel_variants(monkeypatch, kernel, name, K, prec):
         assert rel_fro(got, f64) < TOL_TF32_VS_F64
     else:
         assert rel_fro(got, f64) < TOL_3XTF32_VS_F64
+
+
+def test_concurrent_callers_on_their_own_streams():
+    """Host threads calling the plain and adaptive entry points at once, on
+    their own streams, on shared and separate matrices (the per-matrix state
+    is created under a lock by whichever call comes first): every result
+    equals the single-threaded one bit for bit."""
+    import threading
+    mats = []
+    for seed in (21, 22):
+        n = 8192 + 4096 * seed % 3
+        r, c, v = synth.expand_symmetric(*synth.powerlaw_symmetric(n=n, seed=seed))
+        csr = api.csr_from_coo(n, n, r, c, v)
+        m = device_metcf(csr)
+        a = m.adpbme()
+        mats.append((n, m, a, a.c_rows()))
+    K = 64
+    Bs = [torch.rand((n, K), device="cuda") * 2 - 1 for n, _, _, _ in mats]
+    torch.cuda.synchronize()
+    jobs = [(i % 2, i) for i in range(8)]
+    out = {}
+
+    def work(mi, j):
+        n, m, a, cr = mats[mi]
+        s = torch.cuda.Stream()
+        C = empty_dev(m.c_rows, K)
+        Ca = empty_dev(cr, K)
+        m.spmm(Bs[mi], C, K, stream=s)
+        a.spmm(Bs[mi], Ca, cr, K, stream=s)
+        s.synchronize()
+        out[j] = (C, Ca)
+
+    threads = [threading.Thread(target=work, args=jb) for jb in jobs]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for mi, j in jobs:
+        n, m, a, cr = mats[mi]
+        C = empty_dev(m.c_rows, K)
+        Ca = empty_dev(cr, K)
+        m.spmm(Bs[mi], C, K)
+        a.spmm(Bs[mi], Ca, cr, K)
+        torch.cuda.synchronize()
+        assert torch.equal(out[j][0], C) and torch.equal(out[j][1], Ca)
