@@ -4,7 +4,7 @@ Writes small Matrix Market inputs to ./inputs/, runs the reference's host
 format code on each (oracle/_ref/ref_golden, compiled from the AccSpMM
 sources by `make -C oracle ref`), and stores what it produced as ./<name>.npz:
 COO, CSR, METCF (rowWindowOffset, tcOffset, tcLocalBit, sparseA2B, data),
-AdpBME for the driver's parameters (3, 1, 2, 16) and for (2, 3, 5, 4), and the
+AdpBME for the reference driver's parameters (3, 1, 2, 16; src/mma_tf32.cu:222) and for (2, 3, 5, 4), and the
 balanceStrategy flag.  Run it where the reference sources exist:
 
     make -C oracle ref && python tests/golden/make_golden.py
