@@ -333,6 +333,19 @@ class DeviceMETCF(DeviceObject):
         call("accspmm_spmm_tf32", self.ref, C.c_void_p(_addr(B)), C.c_void_p(_addr(C_out)), K,
              precision, _stream(stream))
 
+    def matmul(self, B, precision: int = capi.PREC_TF32):
+        """A @ B for a CUDA float32 tensor B of cols x K (K a multiple of 4):
+        a new tensor of rows x K, computed on torch's current stream (a view
+        of the 8 * num_windows rows the kernel writes)."""
+        import torch
+        if B.dim() != 2 or B.shape[0] != self.struct.cols or B.dtype != torch.float32 or not B.is_cuda:
+            raise ValueError(f"B must be a CUDA float32 tensor of {self.struct.cols} rows")
+        B = B.contiguous()
+        K = int(B.shape[1])
+        out = torch.empty((self.c_rows, K), device=B.device, dtype=torch.float32)
+        self.spmm(B, out, K, precision, torch.cuda.current_stream(B.device))
+        return out[: self.struct.rows]
+
     def spmm_bias_act(self, B, C_out, K: int, bias=None, activation: int = capi.ACT_NONE,
                       precision: int = capi.PREC_TF32, stream=None) -> None:
         """C_out = act(A * B + bias) with the epilogue fused into the C store."""

@@ -479,3 +479,19 @@ def test_concurrent_callers_on_their_own_streams():
         a.spmm(Bs[mi], Ca, cr, K)
         torch.cuda.synchronize()
         assert torch.equal(out[j][0], C) and torch.equal(out[j][1], Ca)
+
+
+def test_matmul_returns_a_tensor():
+    """DeviceMETCF.matmul: the PyTorch-facing form of the plain entry point."""
+    g = gold("rand203")
+    csr = csr_of_gold(g)
+    m = device_metcf(csr)
+    B = torch.rand((csr["cols"], 36), device="cuda") * 2 - 1
+    C = m.matmul(B)
+    assert tuple(C.shape) == (csr["rows"], 36)
+    D = empty_dev(m.c_rows, 36)
+    m.spmm(B, D, 36)
+    torch.cuda.synchronize()
+    assert torch.equal(C, D[:csr["rows"]])
+    with pytest.raises(ValueError):
+        m.matmul(B[:10])
