@@ -495,3 +495,34 @@ def test_matmul_returns_a_tensor():
     assert torch.equal(C, D[:csr["rows"]])
     with pytest.raises(ValueError):
         m.matmul(B[:10])
+
+
+@pytest.mark.slow
+def test_products_past_32_bit_element_offsets():
+    """cols * K and rows * K beyond 2^32 elements (33.6 M rows at K = 128, a 17 GB
+    B and C): every offset into B and C is a 64-bit product (the reference's
+    32-bit `vint` offsets wrap there).  One entry per row, value 1, at column
+    (7919 i) mod n, and B values exact in TF32, so C[i] must equal
+    B[(7919 i) mod n] bit for bit -- checked on sampled rows, all rows past
+    row 2^25 (whose offsets exceed 2^32) and the rows around that boundary."""
+    n, K = (1 << 25) + 1024, 128
+    i = np.arange(n, dtype=np.int64)
+    col = ((i * 7919) % n).astype(np.uint32)
+    csr = dict(rows=n, cols=n, nnz=n, row_ptr=np.arange(n + 1, dtype=np.uint32), col_idx=col,
+               data=np.ones(n, np.float32))
+    m = device_metcf(csr)
+    r = (torch.arange(n, device="cuda", dtype=torch.int32) % 1000).float()
+    B = torch.empty((n, K), device="cuda")
+    torch.add(r[:, None], torch.arange(K, device="cuda", dtype=torch.float32)[None, :], out=B)
+    B.div_(8)  # integers below 2048 over 8: exact in TF32
+    del r
+    C = empty_dev(m.c_rows, K)
+    m.spmm(B, C, K)
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(1)
+    rows = np.concatenate([rng.integers(0, n, 4096), np.arange((1 << 25) - 8, n)])
+    idx = torch.from_numpy(rows).cuda()
+    want = B[torch.from_numpy(col[rows].astype(np.int64)).cuda()]
+    assert torch.equal(C[idx], want)
+    del B, C
+    torch.cuda.empty_cache()
