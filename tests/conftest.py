@@ -10,4 +10,4 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built library")
-    config.addinivalue_line("markers", "slow: larger CPU cases")
+    config.addinivalue_line("markers", "slow: the larger cases (full-size workloads, maximum sizes)")
