@@ -119,6 +119,7 @@ _SIGS = {
     "accspmm_spmm_tf32": ([C.POINTER(METCF), vp, vp, u32, i32, vp], C.c_int),
     "accspmm_spmm_adaptive": ([C.POINTER(ADPBME), vp, vp, u32, u32, i32, vp], C.c_int),
     "accspmm_device_status": ([vp], C.c_int),
+    "accspmm_selftest_bounded_wait": ([C.c_uint32, vp], C.c_int),
     "accspmm_autotune_metcf": ([C.POINTER(METCF), vp, vp, u32, i32, vp, C.POINTER(TUNE)], C.c_int),
     "accspmm_autotune_clear": ([], None),
     "accspmm_server_create": ([C.POINTER(METCF), u32, C.POINTER(SERVERCFG), C.POINTER(vp)], C.c_int),

@@ -414,6 +414,11 @@ int accspmm_device_status(void* stream) {
     return device_status_impl(stream);
 }
 
+int accspmm_selftest_bounded_wait(uint32_t limit_ms, void* stream) {
+    clear_error();
+    return bounded_wait_selftest(limit_ms, static_cast<cudaStream_t>(stream));
+}
+
 int accspmm_time_spmm(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp, const float* B,
                       float* C, uint32_t c_rows, uint32_t K, int32_t precision, int32_t warmup,
                       int32_t exe, float* avg_ms, void* stream) {

@@ -588,6 +588,34 @@ int launch_bulk(const SpmmArgs& a, int fs, int precision, int nw, int hints, cud
                                             : launch_prec<ACCSPMM_PREC_TF32>(a, fs, nw, hints, s);
 }
 
+namespace {
+
+// The failure path of the bounded waits, exercised on purpose: one warp
+// waits on an mbarrier that nothing arrives on.  The wait gives up after
+// limit_ns, the kernel records ACCSPMM_ERROR_TIMEOUT in the status word and
+// returns; nothing traps and the context stays usable.
+__global__ void bounded_wait_selftest_kernel(uint64_t limit_ns) {
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t b = smem_addr(&bar);
+    if (threadIdx.x == 0) {
+        mbar_init(b, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const bool landed = mbar_wait(b, 0u, limit_ns);  // phase 0 never completes
+    if (!__all_sync(0xffffffffu, landed) && threadIdx.x == 0) atomicOr(&g_bulk_status, 1u);
+}
+
+}  // namespace
+
+int bounded_wait_selftest(uint32_t limit_ms, cudaStream_t s) {
+    if (limit_ms == 0 || limit_ms > 2000)
+        ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "limit_ms must be in [1, 2000]");
+    bounded_wait_selftest_kernel<<<1, 32, 0, s>>>(uint64_t(limit_ms) * 1000000ull);
+    ACC_LAUNCH_CHECK();
+    return ACCSPMM_SUCCESS;
+}
+
 int bulk_status(cudaStream_t s, bool clear) {
     ACC_CUDA(cudaStreamSynchronize(s));
     unsigned int v = 0;

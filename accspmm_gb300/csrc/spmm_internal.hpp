@@ -79,6 +79,8 @@ int adaptive_rwo(const accspmm_adpbme_t* ad, uint32_t W, cudaStream_t s, const u
 int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uint32_t c_rows,
                        uint32_t K, int precision, void* stream);
 int device_status_impl(void* stream);
+// Launches one warp whose bounded wait expires on purpose (spmm_bulk.cu).
+int bounded_wait_selftest(uint32_t limit_ms, cudaStream_t s);
 int spmm_adaptive_noalloc_impl(const accspmm_adpbme_t* ad, const float* B, float* C,
                                uint32_t c_rows, uint32_t K, int precision, void* stream);
 uint32_t noalloc_max_c_rows();

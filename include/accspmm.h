@@ -474,6 +474,13 @@ void accspmm_server_destroy(accspmm_server_t* server);
  * the reference, whose kernels have no asynchronous-copy waits. */
 int accspmm_device_status(void* stream);
 
+/* Self-test of that failure path: launches one warp on `stream` that waits on
+ * an mbarrier nothing arrives on.  Its wait gives up after limit_ms (1 to
+ * 2000) and records ACCSPMM_ERROR_TIMEOUT in the status word, which the next
+ * accspmm_device_status reports and clears; nothing traps and the GPU context
+ * stays usable.  No counterpart in the reference. */
+int accspmm_selftest_bounded_wait(uint32_t limit_ms, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

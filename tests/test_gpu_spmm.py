@@ -526,3 +526,30 @@ def test_products_past_32_bit_element_offsets():
     assert torch.equal(C[idx], want)
     del B, C
     torch.cuda.empty_cache()
+
+
+def test_bounded_wait_failure_path_reports_and_recovers():
+    """A wait that nothing completes (the self-test kernel's mbarrier) gives up
+    after its limit and reports ACCSPMM_ERROR_TIMEOUT through
+    accspmm_device_status, which then clears it; no trap, and the context
+    keeps working (a product computed right after is correct)."""
+    import time
+    capi.call("accspmm_device_status", None)  # start from a clear status
+    t0 = time.perf_counter()
+    capi.call("accspmm_selftest_bounded_wait", 50, None)
+    with pytest.raises(capi.AccSpmmError) as e:
+        capi.call("accspmm_device_status", None)
+    assert e.value.status == capi.ERROR_TIMEOUT
+    assert time.perf_counter() - t0 >= 0.05
+    capi.call("accspmm_device_status", None)  # cleared
+    with pytest.raises(capi.AccSpmmError):
+        capi.call("accspmm_selftest_bounded_wait", 0, None)  # limit out of range
+    g = gold("plsym1000")
+    csr = csr_of_gold(g)
+    m = device_metcf(csr)
+    B = np.random.default_rng(3).uniform(-1, 1, (csr["cols"], 32)).astype(np.float32)
+    C = empty_dev(m.c_rows, 32)
+    m.spmm(torch_dev(B), C, 32)
+    torch.cuda.synchronize()
+    assert rel_fro(C.cpu().numpy()[:csr["rows"]],
+                   oracle.spmm_csr_f64(csr["row_ptr"], csr["col_idx"], csr["data"], B)) < TOL_TF32_VS_F64
