@@ -129,3 +129,23 @@ def test_server_cancel_and_bad_requests(graphs):
     with pytest.raises(capi.AccSpmmError):
         srv.submit(0, B, outs[0], 32, chain=2)  # graph 0 is not square
     srv.destroy()
+
+
+def test_server_wait_limit_and_unknown_request(graphs):
+    """A wait whose limit passes before the request is done returns
+    ACCSPMM_ERROR_TIMEOUT and leaves the request running; waiting again
+    without a limit returns its status.  Requests queue behind a one-slot,
+    one-request budget, so the last of several is still pending when waited
+    for with a zero limit."""
+    m = graphs[3]
+    K = 256
+    need = (m.struct.cols + m.c_rows) * K * 4
+    srv = api.Server(graphs, hbm_budget_bytes=need, max_batch=1, streams=1)
+    B = pinned((m.struct.cols, K), 1.0)
+    outs = [pinned((m.c_rows, K)) for _ in range(6)]
+    ids = [srv.submit(3, B, C, K) for C in outs]
+    assert srv.wait(ids[-1], 0) == capi.ERROR_TIMEOUT
+    assert all(srv.wait(r, -1) == 0 for r in ids)
+    want = plain(m, B, K)
+    assert all(torch.equal(C, want) for C in outs)
+    srv.destroy()
