@@ -553,3 +553,24 @@ def test_bounded_wait_failure_path_reports_and_recovers():
     torch.cuda.synchronize()
     assert rel_fro(C.cpu().numpy()[:csr["rows"]],
                    oracle.spmm_csr_f64(csr["row_ptr"], csr["col_idx"], csr["data"], B)) < TOL_TF32_VS_F64
+
+
+@pytest.mark.slow
+def test_device_builders_match_the_oracle_at_full_size():
+    """The 1M-row power-law matrix (32.2 M entries): the GPU METCF and AdpBME
+    builders equal the oracle's restatement of the reference's host builders
+    array for array, and the GPU balance decision equals the oracle's."""
+    n = 1 << 20
+    rp, ci, vals = synth.powerlaw_local(n=n, seed=0)
+    csr = dict(rows=n, cols=n, nnz=len(ci), row_ptr=rp, col_idx=ci, data=vals)
+    m = device_metcf(csr)
+    o = oracle.metcf(n, rp, ci, vals)
+    h = m.to_numpy()
+    for k in ("rwo", "tc_offset", "bits", "a2b", "data"):
+        np.testing.assert_array_equal(h[k], o[k], err_msg=k)
+    assert m.balance_strategy() == oracle.balance_strategy(o["rwo"])
+    a = m.adpbme().to_numpy()
+    np.testing.assert_array_equal(a["group_offset"], oracle.adpbme_groups(o["rwo"]))
+    np.testing.assert_array_equal(a["row_indices"], oracle.adpbme_row_indices(o["rwo"]))
+    for k in ("tc_offset", "bits", "a2b", "data"):
+        np.testing.assert_array_equal(a[k], o[k], err_msg=k)
