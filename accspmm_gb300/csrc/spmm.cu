@@ -58,6 +58,35 @@ __global__ void __launch_bounds__(NW * 32, MINB) spmm_window_kernel(const SpmmAr
     direct_item<FS, PREC, U, EPI, NW, ROLL>(a, blk);
 }
 
+// The register-direct kernel with the rolling ring reading B from its packed
+// TF32 planes (a.bh, a.bl): bit-identical to spmm_window_kernel<FS, TF32, U,
+// MINB, false, NW, true>, with a quarter fewer gathered sectors.
+template <int FS, int U, int MINB, int NW = kNW>
+__global__ void __launch_bounds__(NW * 32, MINB) spmm_window_packed_kernel(const SpmmArgs a) {
+    extern __shared__ __align__(16) float smem[];
+    float* part = smem;  // [2 * NW] slots
+    uint32_t* s_rwo = reinterpret_cast<uint32_t*>(smem + 2 * NW * 8 * FS);
+    Block<FS, NW> blk;
+    blk.init(a, s_rwo, part);
+    direct_item_packed<FS, U, NW>(a, blk);
+}
+
+// B rounded to TF32 (cvt.rna, as the SpMM's operands are) and split into a
+// plane of bits 31..16 and a plane of bits 15..8, which hold every set bit of
+// the rounded value above bit 12: 3 bytes a value.  One float4 of B per
+// thread and step, read once with a streaming load.
+__global__ void pack_tf32_kernel(const float4* __restrict__ B, uint2* __restrict__ hi,
+                                 uint32_t* __restrict__ lo, size_t n4) {
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n4;
+         i += size_t(gridDim.x) * blockDim.x) {
+        const float4 v = __ldcs(B + i);
+        const uint32_t r0 = f2tf32(v.x), r1 = f2tf32(v.y), r2 = f2tf32(v.z), r3 = f2tf32(v.w);
+        hi[i] = make_uint2((r0 >> 16) | (r1 & 0xFFFF0000u), (r2 >> 16) | (r3 & 0xFFFF0000u));
+        lo[i] = ((r0 >> 8) & 0xFFu) | (((r1 >> 8) & 0xFFu) << 8) | (((r2 >> 8) & 0xFFu) << 16) |
+                (((r3 >> 8) & 0xFFu) << 24);
+    }
+}
+
 // Double-buffered register-direct kernel: the gathers of batch q + 1 are
 // issued before the MMAs of batch q, so every warp keeps a batch of B rows
 // in flight while it computes instead of alternating load and compute phases.
@@ -475,6 +504,25 @@ int launch_direct(const SpmmArgs& a, int occ, int ring, cudaStream_t s) {
     return epi ? launch_direct_t<FS, PREC, U, 2, true>(a, s) : launch_direct_t<FS, PREC, U, 2, false>(a, s);
 }
 
+template <int FS, int U, int MINB>
+int launch_packed_t(const SpmmArgs& a, cudaStream_t s) {
+    const size_t smem = size_t(2 * kNW * 8 * FS) * 4 + size_t(a.wb + 1) * 4;
+    static unsigned attr_set = 0;  // one bit per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 32 && !(attr_set & (1u << dev))) {
+        ACC_CUDA(cudaFuncSetAttribute(spmm_window_packed_kernel<FS, U, MINB>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+        attr_set |= 1u << dev;
+    }
+    const uint64_t grid = uint64_t(a.n_wblocks) * a.n_slices;
+    if (grid == 0) return ACCSPMM_SUCCESS;
+    if (grid > 0x7FFFFFFFull) ACC_FAIL(ACCSPMM_ERROR_OVERFLOW, "grid too large");
+    spmm_window_packed_kernel<FS, U, MINB><<<unsigned(grid), kNW * 32, smem, s>>>(a);
+    ACC_LAUNCH_CHECK();
+    return ACCSPMM_SUCCESS;
+}
+
 }  // namespace
 
 int sm_count() {
@@ -509,16 +557,18 @@ uint32_t slice_width_for(uint32_t w_cfg, uint32_t T, uint32_t K, int precision) 
 int spmm_window_launch(const uint32_t* rwo, const uint32_t* tc_offset, const uint64_t* bits,
                        const uint32_t* a2b, const float* vals, uint32_t W, uint32_t w_cfg,
                        uint32_t T, uint32_t cols, const float* B, float* C, uint32_t K,
-                       int precision, cudaStream_t s, bool stable_rwo) {
+                       int precision, cudaStream_t s, bool stable_rwo, bool allow_pack) {
     return spmm_window_launch_slices(rwo, tc_offset, bits, a2b, vals, W, w_cfg, T, cols, B, C, K,
-                                     precision, 0, 0xFFFFFFFFu, Epilogue{}, s, 0, stable_rwo);
+                                     precision, 0, 0xFFFFFFFFu, Epilogue{}, s, 0, stable_rwo,
+                                     allow_pack);
 }
 
 int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, const uint64_t* bits,
                               const uint32_t* a2b, const float* vals, uint32_t W, uint32_t w_cfg,
                               uint32_t T, uint32_t cols, const float* B, float* C, uint32_t K,
                               int precision, uint32_t slice_begin, uint32_t slice_count,
-                              const Epilogue& epi, cudaStream_t s, int slice_fs, bool stable_rwo) {
+                              const Epilogue& epi, cudaStream_t s, int slice_fs, bool stable_rwo,
+                              bool allow_pack) {
     if (W == 0) return ACCSPMM_SUCCESS;
     // the launch shape depends only on (w_cfg, T, K, precision), so every
     // entry point cuts a matrix into the same pieces and sums partial windows
@@ -543,7 +593,8 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     if (slice_begin >= slices) return ACCSPMM_SUCCESS;
     slice_count = std::min(slice_count, slices - slice_begin);
     SpmmArgs a{rwo, tc_offset, bits, a2b, vals, B, C, W, cols, K, cfg.wb, slice_count,
-               (W + cfg.wb - 1) / cfg.wb, cfg.slice_major, slice_begin, epi.bias, epi.act, nullptr};
+               (W + cfg.wb - 1) / cfg.wb, cfg.slice_major, slice_begin, epi.bias, epi.act, nullptr,
+               nullptr, nullptr};
     // A launch of a few waves ends with its heaviest window blocks: run them
     // first (longest-processing-time order).  Larger launches keep window
     // order, which keeps neighbouring windows' B rows in L2 together.  On the
@@ -576,6 +627,38 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     }
     const bool x3 = precision == ACCSPMM_PREC_3XTF32;
     const int occ = cfg.occ;
+    // TF32 at 128-column slices with the ring: B is first rounded to TF32 and
+    // packed to 3 bytes a value (pack_tf32_kernel), so the SpMM gathers 12 of
+    // every 16 sectors of a row; the MMAs see the same operand bits, so the
+    // results are bit-identical.  On the 1M-row power-law matrix: 2.18 ms per
+    // call (packing included) against 2.29 ms at K = 128, 4.27 against 4.45 ms
+    // at K = 256; at 64-column slices (K = 64) the packing pass cost what the
+    // gathers saved, so those launches read B directly.
+    const int roll = env_int("ACCSPMM_ROLL", cfg.ring);
+    const bool ring_on = roll < 0 || roll != 0;
+    if (allow_pack && !x3 && !(epi.bias || epi.act) && ring_on && cfg.fs == 128 && occ == 2 &&
+        env_int("ACCSPMM_PACK", 1) != 0) {
+        cudaMemPool_t pool;
+        int st = library_pool(&pool);
+        if (st) return st;
+        const size_t n = size_t(cols) * K;  // a multiple of 4
+        void* planes = nullptr;
+        ACC_CUDA(cudaMallocFromPoolAsync(&planes, n * 3 + 64, pool, s));
+        a.bh = static_cast<const uint16_t*>(planes);
+        a.bl = static_cast<const uint8_t*>(planes) + n * 2;
+        const size_t n4 = n / 4;
+        const unsigned blocks = unsigned(std::min<size_t>((n4 + 255) / 256, size_t(sm_count()) * 16));
+        if (n4) {
+            pack_tf32_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(B),
+                                                    static_cast<uint2*>(planes),
+                                                    reinterpret_cast<uint32_t*>(static_cast<uint8_t*>(planes) + n * 2), n4);
+            st = cudaGetLastError() == cudaSuccess ? ACCSPMM_SUCCESS : ACCSPMM_ERROR_CUDA;
+        }
+        if (st == ACCSPMM_SUCCESS) st = launch_packed_t<128, DirectBatch<128>::U, 2>(a, s);
+        cudaFreeAsync(planes, s);
+        if (st) ACC_FAIL(st, "packed SpMM launch failed");
+        return ACCSPMM_SUCCESS;
+    }
     switch (cfg.fs) {
         case 32: return x3 ? launch_direct<32, ACCSPMM_PREC_3XTF32>(a, occ, cfg.ring, s) : launch_direct<32, ACCSPMM_PREC_TF32>(a, occ, cfg.ring, s);
         case 64: return x3 ? launch_direct<64, ACCSPMM_PREC_3XTF32>(a, occ, cfg.ring, s) : launch_direct<64, ACCSPMM_PREC_TF32>(a, occ, cfg.ring, s);
@@ -600,7 +683,7 @@ int spmm_tf32_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t 
     if (st) return st;
     return spmm_window_launch(m->row_window_offset, m->tc_offset, m->tc_local_bit, m->sparse_a2b,
                               m->data, m->num_windows, m->num_windows, m->num_tiles, m->cols, B, C,
-                              K, precision, as_stream(stream), m->owned != 0);
+                              K, precision, as_stream(stream), m->owned != 0, true);
 }
 
 int spmm_bias_act_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K,
@@ -711,7 +794,8 @@ int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uin
         st = cached_rwo(ad, Weff, s, &rwo);
         if (st) return st;
         return spmm_window_launch(rwo, ad->tc_offset, ad->tc_local_bit, ad->sparse_a2b, ad->data, Weff,
-                                  (ad->rows + kWin - 1) / kWin, T, ad->cols, B, C, K, precision, s, true);
+                                  (ad->rows + kWin - 1) / kWin, T, ad->cols, B, C, K, precision, s, true,
+                                  true);
     }
     // a caller-filled object may change between calls: derive every time
     DevBuf<uint32_t> scratch;  // rwo[Weff + 1] then an error word
@@ -722,7 +806,8 @@ int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uin
     rwo_from_row_indices_kernel<<<(Weff + 1 + 255) / 256, 256, 0, s>>>(ad->row_indices, T, Weff, rwo, err);
     ACC_LAUNCH_CHECK();
     return spmm_window_launch(rwo, ad->tc_offset, ad->tc_local_bit, ad->sparse_a2b, ad->data, Weff,
-                              (ad->rows + kWin - 1) / kWin, T, ad->cols, B, C, K, precision, s);
+                              (ad->rows + kWin - 1) / kWin, T, ad->cols, B, C, K, precision, s, false,
+                              true);
 }
 
 // ---------------------------------------------------------------------------

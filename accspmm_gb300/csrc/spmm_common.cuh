@@ -35,6 +35,11 @@ struct SpmmArgs {
     // (No default member initializer: the batched kernel keeps a SpmmArgs in
     // shared memory; brace initialisation without it leaves it null.)
     const uint32_t* order;
+    // B rounded to TF32 and split into two planes (pack_tf32_kernel): bits
+    // 31..16 of each value in bh, bits 15..8 in bl (only 15..13 can be set),
+    // both row-major cols x K.  nullptr: the kernels read B.
+    const uint16_t* bh;
+    const uint8_t* bl;
 };
 
 // TF32 operand rounded to nearest, ties away from zero: the reference's
@@ -80,6 +85,35 @@ __device__ __forceinline__ float ldg_f32_ordered(const float* p) {
 
 __device__ __forceinline__ float comp(const float4& v, int j) {
     return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w;
+}
+
+// Four packed TF32 values of one row of B: halfwords (bits 31..16) in hi,
+// bytes (bits 15..8) in lo.
+struct Packed4 {
+    uint2 hi;
+    uint32_t lo;
+};
+
+__device__ __forceinline__ Packed4 ldg_packed4_ordered(const uint16_t* h, const uint8_t* l) {
+    Packed4 v;
+    asm volatile("ld.global.nc.v2.u32 {%0, %1}, [%2];" : "=r"(v.hi.x), "=r"(v.hi.y) : "l"(h));
+    asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(v.lo) : "l"(l));
+    return v;
+}
+
+// The 32-bit TF32 operand of value j of a Packed4: one byte permute puts
+// halfword j in bits 31..16 and byte j in bits 15..8; bits 7..0 take any
+// byte, and the tensor core reads only bits 31..13, which equal the value's
+// cvt.rna rounding (the packing stored them).
+template <int J>
+__device__ __forceinline__ uint32_t unpack_tf32(const Packed4& v) {
+    constexpr uint32_t lo_b = 4 + J;                 // byte J of the second source
+    constexpr uint32_t hi_b0 = 2 * (J & 1), hi_b1 = hi_b0 + 1;
+    constexpr uint32_t sel = 0u | (lo_b << 4) | (hi_b0 << 8) | (hi_b1 << 12);
+    const uint32_t hw = J < 2 ? v.hi.x : v.hi.y;
+    uint32_t r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(hw), "r"(v.lo), "n"(sel));
+    return r;
 }
 
 // Accumulators of one warp: 8 window rows x FS features.  H = FS / 32 float4
@@ -155,6 +189,38 @@ __device__ __forceinline__ void tile_mma(float (&acc)[Layout<H>::NM][4], const f
             mma_tf32(d, hi[0], hi[1], hi[2], hi[3], bh0, bh1);
             acc[m][0] += d[0]; acc[m][1] += d[1]; acc[m][2] += d[2]; acc[m][3] += d[3];
         }
+    }
+}
+
+// tile_mma for TF32 with B already rounded and packed: the same MMAs on the
+// same operand bits (element j of float4 h of a row is value j of Packed4 h).
+template <int H>
+__device__ __forceinline__ void tile_mma_packed(float (&acc)[Layout<H>::NM][4], const Packed4 (&r0)[H],
+                                                const Packed4 (&r1)[H], float av0, float av1) {
+    constexpr int NM = Layout<H>::NM;
+    const uint32_t b0 = f2tf32(av0), b1 = f2tf32(av1);
+#pragma unroll
+    for (int m = 0; m < NM; ++m) {
+        uint32_t x0, x1, x2, x3;
+        if constexpr (H >= 2) {
+            const int hp = m >> 2, j = m & 3;
+#define ACC_PK(J)                                                     \
+    if (j == J) {                                                     \
+        x0 = unpack_tf32<J>(r0[2 * hp]); x1 = unpack_tf32<J>(r0[2 * hp + 1]); \
+        x2 = unpack_tf32<J>(r1[2 * hp]); x3 = unpack_tf32<J>(r1[2 * hp + 1]); \
+    }
+            ACC_PK(0) ACC_PK(1) ACC_PK(2) ACC_PK(3)
+#undef ACC_PK
+        } else {
+            if (m == 0) {
+                x0 = unpack_tf32<0>(r0[0]); x1 = unpack_tf32<2>(r0[0]);
+                x2 = unpack_tf32<0>(r1[0]); x3 = unpack_tf32<2>(r1[0]);
+            } else {
+                x0 = unpack_tf32<1>(r0[0]); x1 = unpack_tf32<3>(r0[0]);
+                x2 = unpack_tf32<1>(r1[0]); x3 = unpack_tf32<3>(r1[0]);
+            }
+        }
+        mma_tf32(acc[m], x0, x1, x2, x3, b0, b1);
     }
 }
 

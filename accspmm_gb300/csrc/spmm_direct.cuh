@@ -164,4 +164,100 @@ __device__ __forceinline__ void direct_item(const SpmmArgs& a, const Block<FS, N
 }
 
 
+// direct_item with the rolling tile ring for TF32 with B packed (a.bh and
+// a.bl: three bytes a value instead of four, so 12 of every 16 sectors of a
+// gathered row).  Same pieces, same MMAs on the same operand bits, same
+// order: bit-identical to direct_item<FS, TF32, U, false, NW, true>.
+template <int FS, int U, int NW = kDirectNW>
+__device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Block<FS, NW>& blk) {
+    constexpr int H = FS / 32;
+    using L = Layout<H>;
+    constexpr int NM = L::NM;
+    constexpr int MA = (8 * U + 31) / 32;             // a2b registers per lane
+
+    const int lane = blk.lane, g = blk.g, tq = blk.tq;
+    const uint32_t tb = blk.bound(blk.warp), te = blk.bound(blk.warp + 1);
+
+    bool fok[H];
+#pragma unroll
+    for (int h = 0; h < H; ++h) fok[h] = blk.f0 + 32 * h + 4 * g < a.K;
+
+    if (tb < te) {
+        uint32_t wl = blk.window_of(tb);
+        uint32_t next_bound = blk.s_rwo[wl + 1];
+        bool first_win = true;
+        float acc[NM][4];
+#pragma unroll
+        for (int m = 0; m < NM; ++m) acc[m][0] = acc[m][1] = acc[m][2] = acc[m][3] = 0.f;
+
+        uint32_t ma[MA];
+        uint64_t mb;
+        uint32_t mo;
+        auto load_meta = [&](uint32_t t) {
+#pragma unroll
+            for (int j = 0; j < MA; ++j) {
+                uint32_t e = 32 * j + lane;
+                uint32_t tile = t + e / 8;
+                ma[j] = (e < 8 * U && tile < te) ? __ldg(a.a2b + size_t(t) * 8 + e) : kPad;
+            }
+            uint32_t tl = t + uint32_t(lane);
+            bool ok = lane < U && tl < te;
+            mb = ok ? __ldg(reinterpret_cast<const unsigned long long*>(a.bits) + tl) : 0ull;
+            mo = ok ? __ldg(a.tc_offset + tl) : 0u;
+        };
+        load_meta(tb);
+
+        BitDecode dec;
+        dec.init(g, tq);
+        const uint16_t* Hl = a.bh + blk.f0 + 4 * g;
+        const uint8_t* Ll = a.bl + blk.f0 + 4 * g;
+        float av0[U], av1[U];
+        Packed4 r0[U][H], r1[U][H];
+        auto issue = [&](int u) {
+            const uint32_t i0 = __shfl_sync(0xffffffffu, ma[(8 * u) / 32], (8 * u + tq) & 31);
+            const uint32_t i1 = __shfl_sync(0xffffffffu, ma[(8 * u) / 32], (8 * u + tq + 4) & 31);
+            const uint64_t bm = shfl_u64(mb, u);
+            const uint32_t to = __shfl_sync(0xffffffffu, mo, u);
+            uint32_t x0, x1;
+            bool q0, q1;
+            dec.decode(bm, x0, x1, q0, q1);
+            av0[u] = q0 ? ldg_f32_ordered(a.vals + to + x0) : 0.f;
+            av1[u] = q1 ? ldg_f32_ordered(a.vals + to + x1) : 0.f;
+            const bool v0 = i0 < a.cols, v1 = i1 < a.cols;
+            const size_t o0 = size_t(v0 ? i0 : 0) * a.K, o1 = size_t(v1 ? i1 : 0) * a.K;
+#pragma unroll
+            for (int h = 0; h < H; ++h) {
+                const Packed4 zero{make_uint2(0u, 0u), 0u};
+                r0[u][h] = (v0 && fok[h]) ? ldg_packed4_ordered(Hl + o0 + 32 * h, Ll + o0 + 32 * h) : zero;
+                r1[u][h] = (v1 && fok[h]) ? ldg_packed4_ordered(Hl + o1 + 32 * h, Ll + o1 + 32 * h) : zero;
+            }
+        };
+#pragma unroll
+        for (int u = 0; u < U; ++u) issue(u);
+        load_meta(tb + U);  // padding when past te
+        for (uint32_t t = tb; t < te; t += U) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint32_t tt = t + u;
+                if (tt < te) {
+                    if (tt >= next_bound) {
+                        blk.template flush<false>(a, acc, wl, tb, te, first_win);
+                        first_win = false;
+#pragma unroll
+                        for (int m = 0; m < NM; ++m) acc[m][0] = acc[m][1] = acc[m][2] = acc[m][3] = 0.f;
+                        while (blk.s_rwo[wl + 1] <= tt) ++wl;
+                        next_bound = blk.s_rwo[wl + 1];
+                    }
+                    tile_mma_packed<H>(acc, r0[u], r1[u], av0[u], av1[u]);
+                }
+                issue(u);  // tile t + U + u
+            }
+            load_meta(t + 2 * U);
+        }
+        blk.template flush<false>(a, acc, wl, tb, te, first_win);
+    }
+    __syncthreads();
+    blk.template finish<false>(a);
+}
+
 }  // namespace accspmm

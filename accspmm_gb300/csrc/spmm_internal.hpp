@@ -18,11 +18,14 @@ uint32_t window_block_for(uint32_t w_cfg, uint32_t T, uint32_t K, int precision)
 // the launch shape is chosen from (w_cfg, T, K, precision).
 // stable_rwo: rwo belongs to a library-owned matrix and stays unchanged
 // until schedule_cache_forget(rwo), so a heaviest-first block schedule may be
-// computed once and kept for it.
+// computed once and kept for it.  allow_pack: the launch may pack B into TF32
+// planes in a buffer from the library's pool first (TF32 shapes with the
+// rolling ring).
 int spmm_window_launch(const uint32_t* rwo, const uint32_t* tc_offset, const uint64_t* bits,
                        const uint32_t* a2b, const float* vals, uint32_t W, uint32_t w_cfg,
                        uint32_t T, uint32_t cols, const float* B, float* C, uint32_t K,
-                       int precision, cudaStream_t s, bool stable_rwo = false);
+                       int precision, cudaStream_t s, bool stable_rwo = false,
+                       bool allow_pack = false);
 // Drops the block schedules kept for these window offsets (before they are freed).
 void schedule_cache_forget(const uint32_t* rwo);
 // Epilogue applied when C is stored: C = act(A B + bias[col]).
@@ -39,7 +42,7 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
                               uint32_t T, uint32_t cols, const float* B, float* C, uint32_t K,
                               int precision, uint32_t slice_begin, uint32_t slice_count,
                               const Epilogue& epi, cudaStream_t s, int slice_fs,
-                              bool stable_rwo = false);
+                              bool stable_rwo = false, bool allow_pack = false);
 // Slice width, CTAs per SM (register-direct kernel) and windows per CTA the
 // launch-shape chooser picks.
 void launch_shape_for(uint32_t w_cfg, uint32_t T, uint32_t K, int precision, int* fs, int* occ,

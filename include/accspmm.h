@@ -243,7 +243,10 @@ void accspmm_adpbme_destroy(accspmm_adpbme_t* adp);
  * the blocks on the GPU, waits for that on the host once, and keeps the
  * schedule until accspmm_metcf_destroy (results do not depend on it).
  * Calls may be captured into a CUDA graph; a call captured before the
- * schedule exists runs the blocks in window order. */
+ * schedule exists runs the blocks in window order.  In TF32 with K > 64 a
+ * call first rounds B to TF32 and packs it to 3 bytes a value in a buffer of
+ * 3 cols K bytes from the library's memory pool (released in stream order):
+ * the SpMM then gathers a quarter fewer bytes, with bit-identical results. */
 int accspmm_spmm_tf32(const accspmm_metcf_t* metcf, const float* B, float* C,
                       uint32_t K, int32_t precision, void* stream);
 
@@ -259,7 +262,7 @@ int accspmm_spmm_tf32(const accspmm_metcf_t* metcf, const float* B, float* C,
  * and waits for them on the host once, and must not be captured into a CUDA
  * graph (it returns ACCSPMM_ERROR_UNSUPPORTED inside a capture); later calls
  * may be captured.  For an AdpBME the caller filled they are derived into
- * stream-ordered scratch on every call. */
+ * stream-ordered scratch on every call.  B is packed as in accspmm_spmm_tf32. */
 int accspmm_spmm_adaptive(const accspmm_adpbme_t* adp, const float* B,
                           float* C, uint32_t c_rows, uint32_t K,
                           int32_t precision, void* stream);

@@ -574,3 +574,30 @@ def test_device_builders_match_the_oracle_at_full_size():
     np.testing.assert_array_equal(a["row_indices"], oracle.adpbme_row_indices(o["rwo"]))
     for k in ("tc_offset", "bits", "a2b", "data"):
         np.testing.assert_array_equal(a[k], o[k], err_msg=k)
+
+
+@pytest.mark.parametrize("K", [68, 128, 256])
+def test_packed_b_is_bit_identical(monkeypatch, K):
+    """TF32 launches at 128-column slices first pack B to 3 bytes a value
+    (rounded to TF32 and split in two planes); the SpMM on the packed planes
+    returns bitwise what the kernel reading B directly returns, on the plain
+    and adaptive entry points, and within the TF32 tolerance of FP64."""
+    g = gold("plsym1000")
+    csr = csr_of_gold(g)
+    m = device_metcf(csr)
+    a = m.adpbme()
+    cr = a.c_rows()
+    B = np.random.default_rng(K).uniform(-1, 1, (csr["cols"], K)).astype(np.float32)
+    dB = torch_dev(B)
+    out = {}
+    for pk in ("1", "0"):
+        monkeypatch.setenv("ACCSPMM_PACK", pk)
+        C, Ca = empty_dev(m.c_rows, K), empty_dev(cr, K)
+        m.spmm(dB, C, K)
+        a.spmm(dB, Ca, cr, K)
+        torch.cuda.synchronize()
+        out[pk] = (C, Ca)
+    assert torch.equal(out["1"][0], out["0"][0]) and torch.equal(out["1"][1], out["0"][1])
+    got = out["1"][0].cpu().numpy()[:csr["rows"]]
+    ref = oracle.spmm_csr_f64(csr["row_ptr"], csr["col_idx"], csr["data"], B)
+    assert rel_fro(got, ref) < TOL_TF32_VS_F64
