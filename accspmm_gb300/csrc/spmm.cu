@@ -633,11 +633,14 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     // results are bit-identical.  On the 1M-row power-law matrix: 2.18 ms per
     // call (packing included) against 2.29 ms at K = 128, 4.27 against 4.45 ms
     // at K = 256; at 64-column slices (K = 64) the packing pass cost what the
-    // gathers saved, so those launches read B directly.
+    // gathers saved, and for a B that fits the L2 (the 16,384-row matrix,
+    // 53.5 against 52.0 us) it only adds a pass, so those launches read B
+    // directly.
     const int roll = env_int("ACCSPMM_ROLL", cfg.ring);
     const bool ring_on = roll < 0 || roll != 0;
+    const bool b_past_l2 = uint64_t(cols) * K * 4 >= (uint64_t(128) << 20);
     if (allow_pack && !x3 && !(epi.bias || epi.act) && ring_on && cfg.fs == 128 && occ == 2 &&
-        env_int("ACCSPMM_PACK", 1) != 0) {
+        b_past_l2 && env_int("ACCSPMM_PACK", 1) != 0) {
         cudaMemPool_t pool;
         int st = library_pool(&pool);
         if (st) return st;

@@ -243,8 +243,9 @@ void accspmm_adpbme_destroy(accspmm_adpbme_t* adp);
  * the blocks on the GPU, waits for that on the host once, and keeps the
  * schedule until accspmm_metcf_destroy (results do not depend on it).
  * Calls may be captured into a CUDA graph; a call captured before the
- * schedule exists runs the blocks in window order.  In TF32 with K > 64 a
- * call first rounds B to TF32 and packs it to 3 bytes a value in a buffer of
+ * schedule exists runs the blocks in window order.  In TF32 with K > 64 and
+ * a B of at least 128 MiB a call first rounds B to TF32 and packs it to
+ * 3 bytes a value in a buffer of
  * 3 cols K bytes from the library's memory pool (released in stream order):
  * the SpMM then gathers a quarter fewer bytes, with bit-identical results. */
 int accspmm_spmm_tf32(const accspmm_metcf_t* metcf, const float* B, float* C,

@@ -576,19 +576,20 @@ def test_device_builders_match_the_oracle_at_full_size():
         np.testing.assert_array_equal(a[k], o[k], err_msg=k)
 
 
-@pytest.mark.parametrize("K", [68, 128, 256])
+@pytest.mark.parametrize("K", [136, 256])
 def test_packed_b_is_bit_identical(monkeypatch, K):
-    """TF32 launches at 128-column slices first pack B to 3 bytes a value
-    (rounded to TF32 and split in two planes); the SpMM on the packed planes
-    returns bitwise what the kernel reading B directly returns, on the plain
-    and adaptive entry points, and within the TF32 tolerance of FP64."""
-    g = gold("plsym1000")
-    csr = csr_of_gold(g)
+    """TF32 launches at 128-column slices whose B is at least 128 MiB first
+    pack B to 3 bytes a value (rounded to TF32 and split in two planes); the
+    SpMM on the packed planes returns bitwise what the kernel reading B
+    directly returns, on the plain and adaptive entry points, within the TF32
+    tolerance of FP64 on sampled rows."""
+    n = 1 << 18
+    rp, ci, vals = synth.powerlaw_local(n=n, seed=4)
+    csr = dict(rows=n, cols=n, nnz=len(ci), row_ptr=rp, col_idx=ci, data=vals)
     m = device_metcf(csr)
     a = m.adpbme()
     cr = a.c_rows()
-    B = np.random.default_rng(K).uniform(-1, 1, (csr["cols"], K)).astype(np.float32)
-    dB = torch_dev(B)
+    dB = torch.rand((n, K), device="cuda") * 2 - 1
     out = {}
     for pk in ("1", "0"):
         monkeypatch.setenv("ACCSPMM_PACK", pk)
@@ -598,6 +599,10 @@ def test_packed_b_is_bit_identical(monkeypatch, K):
         torch.cuda.synchronize()
         out[pk] = (C, Ca)
     assert torch.equal(out["1"][0], out["0"][0]) and torch.equal(out["1"][1], out["0"][1])
-    got = out["1"][0].cpu().numpy()[:csr["rows"]]
-    ref = oracle.spmm_csr_f64(csr["row_ptr"], csr["col_idx"], csr["data"], B)
+    rows = np.sort(np.random.default_rng(K).choice(n, 2048, replace=False))
+    sub_rp = np.concatenate([[0], np.cumsum(np.diff(rp.astype(np.int64))[rows])]).astype(np.uint32)
+    sub_ci = np.concatenate([ci[rp[r]:rp[r + 1]] for r in rows])
+    sub_v = np.concatenate([vals[rp[r]:rp[r + 1]] for r in rows])
+    ref = oracle.spmm_csr_f64(sub_rp, sub_ci, sub_v, dB.cpu().numpy())
+    got = out["1"][0][torch.from_numpy(rows).cuda()].cpu().numpy()
     assert rel_fro(got, ref) < TOL_TF32_VS_F64
