@@ -390,7 +390,7 @@ class DeviceMETCF(DeviceObject):
              K, precision, _stream(stream), C.byref(r))
         return dict(kernel={0: "direct", 4: "double-buffered"}.get(r.kernel, str(r.kernel)),
                     slice_width=r.slice_width, windows_per_cta=r.windows_per_cta,
-                    ctas_per_sm=r.ctas_per_sm, tile_ring=r.tile_ring, best_ms=round(r.best_ms, 4),
+                    ctas_per_sm=r.ctas_per_sm, tile_ring=r.tile_ring, packed_b=r.packed_b, best_ms=round(r.best_ms, 4),
                     default_ms=round(r.default_ms, 4), candidates=r.candidates)
 
 

@@ -72,7 +72,7 @@ class ADPBME(C.Structure):
 class TUNE(C.Structure):
     _fields_ = [("kernel", i32), ("slice_width", u32), ("windows_per_cta", u32),
                 ("best_ms", C.c_float), ("default_ms", C.c_float), ("candidates", u32),
-                ("ctas_per_sm", u32), ("tile_ring", i32)]
+                ("ctas_per_sm", u32), ("tile_ring", i32), ("packed_b", i32)]
 
 
 class SERVERCFG(C.Structure):

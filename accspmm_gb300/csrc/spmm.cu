@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) spmm_window_kernel(const SpmmAr
 }
 
 // The register-direct kernel with the rolling ring reading B from its packed
-// TF32 planes (a.bh, a.bl): bit-identical to spmm_window_kernel<FS, TF32, U,
+// TF32 rows (a.bp): bit-identical to spmm_window_kernel<FS, TF32, U,
 // MINB, false, NW, true>, with a quarter fewer gathered sectors.
 template <int FS, int U, int MINB, int NW = kNW>
 __global__ void __launch_bounds__(NW * 32, MINB) spmm_window_packed_kernel(const SpmmArgs a) {
@@ -71,19 +71,27 @@ __global__ void __launch_bounds__(NW * 32, MINB) spmm_window_packed_kernel(const
     direct_item_packed<FS, U, NW>(a, blk);
 }
 
-// B rounded to TF32 (cvt.rna, as the SpMM's operands are) and split into a
-// plane of bits 31..16 and a plane of bits 15..8, which hold every set bit of
-// the rounded value above bit 12: 3 bytes a value.  One float4 of B per
-// thread and step, read once with a streaming load.
-__global__ void pack_tf32_kernel(const float4* __restrict__ B, uint2* __restrict__ hi,
-                                 uint32_t* __restrict__ lo, size_t n4) {
+// B rounded to TF32 (cvt.rna, as the SpMM's operands are) and packed row by
+// row: K halfwords of bits 31..16, then K bytes of bits 15..8, which hold
+// every set bit of the rounded value above bit 12 -- 3 bytes a value, a row
+// one contiguous run of `pitch` bytes (3K rounded up to 16), so that a
+// gathered row stays in one DRAM page.  One float4 of B per thread and step,
+// read once with a streaming load.
+__global__ void pack_tf32_kernel(const float4* __restrict__ B, uint8_t* __restrict__ P, uint32_t K,
+                                 uint32_t pitch, size_t n4) {
+    const uint32_t k4 = K / 4;
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n4;
          i += size_t(gridDim.x) * blockDim.x) {
+        const size_t row = i / k4;
+        const uint32_t c = uint32_t(i - row * k4) * 4;
         const float4 v = __ldcs(B + i);
         const uint32_t r0 = f2tf32(v.x), r1 = f2tf32(v.y), r2 = f2tf32(v.z), r3 = f2tf32(v.w);
-        hi[i] = make_uint2((r0 >> 16) | (r1 & 0xFFFF0000u), (r2 >> 16) | (r3 & 0xFFFF0000u));
-        lo[i] = ((r0 >> 8) & 0xFFu) | (((r1 >> 8) & 0xFFu) << 8) | (((r2 >> 8) & 0xFFu) << 16) |
-                (((r3 >> 8) & 0xFFu) << 24);
+        uint8_t* base = P + row * pitch;
+        *reinterpret_cast<uint2*>(base + 2 * c) =
+            make_uint2((r0 >> 16) | (r1 & 0xFFFF0000u), (r2 >> 16) | (r3 & 0xFFFF0000u));
+        *reinterpret_cast<uint32_t*>(base + 2 * K + c) =
+            ((r0 >> 8) & 0xFFu) | (((r1 >> 8) & 0xFFu) << 8) | (((r2 >> 8) & 0xFFu) << 16) |
+            (((r3 >> 8) & 0xFFu) << 24);
     }
 }
 
@@ -375,6 +383,7 @@ struct Config {
     int hints;
     uint32_t wb;
     uint32_t slice_major;
+    int pack;  // TF32 ring at 128-column slices: gather from a packed copy of B (-1 by the default rule, 0 off, 1 on)
 };
 
 int env_int(const char* name, int dflt) {
@@ -419,6 +428,7 @@ Config choose_config(uint32_t W, uint32_t T, uint32_t K, int precision) {
     c.nw = c.fs == 32 ? 8 : 4;
     c.hints = 1;
     c.slice_major = 0;
+    c.pack = -1;
     {
         uint64_t slices = (K + c.fs - 1) / c.fs;
         uint64_t want = uint64_t(sm_count()) * 4;
@@ -448,6 +458,9 @@ Config choose_config(uint32_t W, uint32_t T, uint32_t K, int precision) {
     c.hints = env_int("ACCSPMM_HINTS", c.hints) ? 1 : 0;
     int wbe = env_int("ACCSPMM_WB", 0);
     if (wbe >= 1 && wbe <= 1024) c.wb = uint32_t(wbe);
+    const int pk = env_int("ACCSPMM_PACK", -1);  // 0 never pack B, 2 pack wherever the launch shape allows
+    if (pk == 0) c.pack = 0;
+    if (pk == 2) c.pack = 1;
     if (const char* e = std::getenv("ACCSPMM_ORDER")) c.slice_major = std::strcmp(e, "slice") == 0;
     return c;
 }
@@ -594,7 +607,7 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     slice_count = std::min(slice_count, slices - slice_begin);
     SpmmArgs a{rwo, tc_offset, bits, a2b, vals, B, C, W, cols, K, cfg.wb, slice_count,
                (W + cfg.wb - 1) / cfg.wb, cfg.slice_major, slice_begin, epi.bias, epi.act, nullptr,
-               nullptr, nullptr};
+               nullptr, 0};
     // A launch of a few waves ends with its heaviest window blocks: run them
     // first (longest-processing-time order).  Larger launches keep window
     // order, which keeps neighbouring windows' B rows in L2 together.  On the
@@ -631,34 +644,37 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     // packed to 3 bytes a value (pack_tf32_kernel), so the SpMM gathers 12 of
     // every 16 sectors of a row; the MMAs see the same operand bits, so the
     // results are bit-identical.  On the 1M-row power-law matrix: 2.18 ms per
-    // call (packing included) against 2.29 ms at K = 128, 4.27 against 4.45 ms
-    // at K = 256; at 64-column slices (K = 64) the packing pass cost what the
-    // gathers saved, and for a B that fits the L2 (the 16,384-row matrix,
-    // 53.5 against 52.0 us) it only adds a pass, so those launches read B
-    // directly.
+    // call (packing included) against 2.30 ms at K = 128, 4.27 against 4.45 ms
+    // at K = 256.  The default rule packs a B of 128 MiB to 1 GiB: at 64-column
+    // slices (K = 64) the packing pass cost what the gathers saved; a B that
+    // fits the L2 (the 16,384-row matrix, 53.5 against 52.0 us) only gains a
+    // pass; and the larger the B against the L2, the less of the gain from
+    // holding more rows there is left while the pass (7 bytes a value) grows:
+    // on the 2M-row GCN graph at K = 256 (a 2 GiB B) the packed call took
+    // 7.61 ms against 7.46.  The autotuner times both ways.
     const int roll = env_int("ACCSPMM_ROLL", cfg.ring);
     const bool ring_on = roll < 0 || roll != 0;
-    const bool b_past_l2 = uint64_t(cols) * K * 4 >= (uint64_t(128) << 20);
-    if (allow_pack && !x3 && !(epi.bias || epi.act) && ring_on && cfg.fs == 128 && occ == 2 &&
-        b_past_l2 && env_int("ACCSPMM_PACK", 1) != 0) {
+    const uint64_t b_bytes = uint64_t(cols) * K * 4;
+    const bool pack_rule = cfg.pack > 0 ||
+                           (cfg.pack < 0 && b_bytes >= (uint64_t(128) << 20) && b_bytes <= (uint64_t(1) << 30));
+    if (allow_pack && !x3 && !(epi.bias || epi.act) && ring_on && cfg.fs == 128 && occ == 2 && pack_rule) {
         cudaMemPool_t pool;
         int st = library_pool(&pool);
         if (st) return st;
-        const size_t n = size_t(cols) * K;  // a multiple of 4
-        void* planes = nullptr;
-        ACC_CUDA(cudaMallocFromPoolAsync(&planes, n * 3 + 64, pool, s));
-        a.bh = static_cast<const uint16_t*>(planes);
-        a.bl = static_cast<const uint8_t*>(planes) + n * 2;
-        const size_t n4 = n / 4;
+        const uint32_t pitch = (3 * K + 15) / 16 * 16;
+        void* packed = nullptr;
+        ACC_CUDA(cudaMallocFromPoolAsync(&packed, size_t(cols) * pitch + 64, pool, s));
+        a.bp = static_cast<const uint8_t*>(packed);
+        a.bpitch = pitch;
+        const size_t n4 = size_t(cols) * (K / 4);
         const unsigned blocks = unsigned(std::min<size_t>((n4 + 255) / 256, size_t(sm_count()) * 16));
         if (n4) {
             pack_tf32_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(B),
-                                                    static_cast<uint2*>(planes),
-                                                    reinterpret_cast<uint32_t*>(static_cast<uint8_t*>(planes) + n * 2), n4);
+                                                    static_cast<uint8_t*>(packed), K, pitch, n4);
             st = cudaGetLastError() == cudaSuccess ? ACCSPMM_SUCCESS : ACCSPMM_ERROR_CUDA;
         }
         if (st == ACCSPMM_SUCCESS) st = launch_packed_t<128, DirectBatch<128>::U, 2>(a, s);
-        cudaFreeAsync(planes, s);
+        cudaFreeAsync(packed, s);
         if (st) ACC_FAIL(st, "packed SpMM launch failed");
         return ACCSPMM_SUCCESS;
     }
@@ -904,7 +920,13 @@ int autotune_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K
                 c.fs = fs;
                 c.wb = wb;
                 c.slice_major = 0;
+                c.pack = 0;
                 cand.push_back(c);
+                // TF32 with the ring at 128-column slices: also gathering from a packed B
+                if (precision == ACCSPMM_PREC_TF32 && c.kernel == kDirect && c.occ == 2 && c.ring == 1 && fs == 128) {
+                    c.pack = 1;
+                    cand.push_back(c);
+                }
             }
         }
     cudaEvent_t e0, e1;
@@ -955,6 +977,7 @@ int autotune_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K
         out->best_ms = best_ms;
         out->default_ms = dflt_ms;
         out->candidates = uint32_t(cand.size()) + 1;
+        out->packed_b = best.pack;
     }
     return ACCSPMM_SUCCESS;
 }

@@ -63,7 +63,7 @@ spmm_batch_kernel(const BatchDesc* __restrict__ desc, uint32_t n_desc, uint32_t 
                 const uint32_t local = item - d.item0;
                 s_args = SpmmArgs{d.rwo, d.tc_offset, d.bits, d.a2b, d.vals, d.B, d.C, d.W, d.cols,
                                   d.K, d.wb, d.n_slices, d.n_wblocks, 0, 0, nullptr, 0, nullptr,
-                                  nullptr, nullptr};
+                                  nullptr, 0};
                 s_wbk = local / d.n_slices;
                 s_slice = local - s_wbk * d.n_slices;
             }

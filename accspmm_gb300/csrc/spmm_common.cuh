@@ -35,11 +35,12 @@ struct SpmmArgs {
     // (No default member initializer: the batched kernel keeps a SpmmArgs in
     // shared memory; brace initialisation without it leaves it null.)
     const uint32_t* order;
-    // B rounded to TF32 and split into two planes (pack_tf32_kernel): bits
-    // 31..16 of each value in bh, bits 15..8 in bl (only 15..13 can be set),
-    // both row-major cols x K.  nullptr: the kernels read B.
-    const uint16_t* bh;
-    const uint8_t* bl;
+    // B rounded to TF32 and packed (pack_tf32_kernel): row i at bp + i * bpitch
+    // bytes holds bits 31..16 of its K values as K halfwords, then bits 15..8
+    // (only 15..13 can be set) as K bytes, so a gathered row is one contiguous
+    // run.  nullptr: the kernels read B.
+    const uint8_t* bp;
+    uint32_t bpitch;
 };
 
 // TF32 operand rounded to nearest, ties away from zero: the reference's
@@ -94,7 +95,7 @@ struct Packed4 {
     uint32_t lo;
 };
 
-__device__ __forceinline__ Packed4 ldg_packed4_ordered(const uint16_t* h, const uint8_t* l) {
+__device__ __forceinline__ Packed4 ldg_packed4_ordered(const uint8_t* h, const uint8_t* l) {
     Packed4 v;
     asm volatile("ld.global.nc.v2.u32 {%0, %1}, [%2];" : "=r"(v.hi.x), "=r"(v.hi.y) : "l"(h));
     asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(v.lo) : "l"(l));

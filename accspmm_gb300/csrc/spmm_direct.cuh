@@ -164,9 +164,9 @@ __device__ __forceinline__ void direct_item(const SpmmArgs& a, const Block<FS, N
 }
 
 
-// direct_item with the rolling tile ring for TF32 with B packed (a.bh and
-// a.bl: three bytes a value instead of four, so 12 of every 16 sectors of a
-// gathered row).  Same pieces, same MMAs on the same operand bits, same
+// direct_item with the rolling tile ring for TF32 with B packed (a.bp, rows
+// of a.bpitch bytes: three bytes a value instead of four, so 12 of every 16
+// sectors of a gathered row).  Same pieces, same MMAs on the same operand bits, same
 // order: bit-identical to direct_item<FS, TF32, U, false, NW, true>.
 template <int FS, int U, int NW = kDirectNW>
 __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Block<FS, NW>& blk) {
@@ -209,8 +209,9 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
 
         BitDecode dec;
         dec.init(g, tq);
-        const uint16_t* Hl = a.bh + blk.f0 + 4 * g;
-        const uint8_t* Ll = a.bl + blk.f0 + 4 * g;
+        // this lane's first value of a row: halfword f0 + 4g, byte 2K + f0 + 4g
+        const uint8_t* Pl = a.bp + 2 * (blk.f0 + 4 * g);
+        const size_t lo_off = size_t(2) * a.K - (blk.f0 + 4 * g);
         float av0[U], av1[U];
         Packed4 r0[U][H], r1[U][H];
         auto issue = [&](int u) {
@@ -224,12 +225,14 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
             av0[u] = q0 ? ldg_f32_ordered(a.vals + to + x0) : 0.f;
             av1[u] = q1 ? ldg_f32_ordered(a.vals + to + x1) : 0.f;
             const bool v0 = i0 < a.cols, v1 = i1 < a.cols;
-            const size_t o0 = size_t(v0 ? i0 : 0) * a.K, o1 = size_t(v1 ? i1 : 0) * a.K;
+            const uint8_t* w0 = Pl + size_t(v0 ? i0 : 0) * a.bpitch;
+            const uint8_t* w1 = Pl + size_t(v1 ? i1 : 0) * a.bpitch;
 #pragma unroll
             for (int h = 0; h < H; ++h) {
                 const Packed4 zero{make_uint2(0u, 0u), 0u};
-                r0[u][h] = (v0 && fok[h]) ? ldg_packed4_ordered(Hl + o0 + 32 * h, Ll + o0 + 32 * h) : zero;
-                r1[u][h] = (v1 && fok[h]) ? ldg_packed4_ordered(Hl + o1 + 32 * h, Ll + o1 + 32 * h) : zero;
+                // halfwords at w + 64 h, bytes at w + lo_off + 32 h
+                r0[u][h] = (v0 && fok[h]) ? ldg_packed4_ordered(w0 + 64 * h, w0 + lo_off + 32 * h) : zero;
+                r1[u][h] = (v1 && fok[h]) ? ldg_packed4_ordered(w1 + 64 * h, w1 + lo_off + 32 * h) : zero;
             }
         };
 #pragma unroll

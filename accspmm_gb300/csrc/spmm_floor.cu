@@ -122,7 +122,7 @@ int gather_floor_impl(const accspmm_metcf_t* m, const float* B, uint32_t K, uint
     const uint32_t W = m->num_windows;
     SpmmArgs a{m->row_window_offset, m->tc_offset, m->tc_local_bit, m->sparse_a2b, m->data, B,
                nullptr, W, m->cols, K, wb, (K + uint32_t(fs) - 1) / uint32_t(fs), (W + wb - 1) / wb,
-               0, 0, nullptr, 0, nullptr, nullptr, nullptr};
+               0, 0, nullptr, 0, nullptr, nullptr, 0};
     DevBuf<float> sink;
     ACC_CUDA(sink.alloc(1, s));
     int r = launch_floor_shape(a, fs, occ, sink.p, s);  // warm-up

@@ -448,10 +448,14 @@ def run_ours(args):
             m.spmm(Bt, Ct, K, prec, stream)
 
     # per step: the SpMM launch, preceded for TF32 at 128-column slices
-    # (K > 64) with a B of at least 128 MiB by the launch that packs B to
-    # TF32 planes; the adaptive path's
-    # window offsets are derived once per AdpBME (during the warm-up) and kept
-    launches_per_step = 2 if (prec == capi.PREC_TF32 and K > 64 and n * K * 4 >= (128 << 20)
+    # (K > 64) with a B of 128 MiB to 1 GiB (the library's default rule, or
+    # as the tuned shape says) by the launch that packs B to TF32; the
+    # adaptive path's window offsets are derived once per AdpBME (during the
+    # warm-up) and kept
+    pack_rule = K > 64 and (128 << 20) <= n * K * 4 <= (1 << 30)
+    if tune is not None and tune["packed_b"] >= 0:
+        pack_rule = tune["packed_b"] == 1
+    launches_per_step = 2 if (prec == capi.PREC_TF32 and pack_rule
                               and os.environ.get("ACCSPMM_PACK", "1") != "0") else 1
     for _ in range(max(args.warmup, 3)):
         step(B, C)

@@ -244,10 +244,11 @@ void accspmm_adpbme_destroy(accspmm_adpbme_t* adp);
  * schedule until accspmm_metcf_destroy (results do not depend on it).
  * Calls may be captured into a CUDA graph; a call captured before the
  * schedule exists runs the blocks in window order.  In TF32 with K > 64 and
- * a B of at least 128 MiB a call first rounds B to TF32 and packs it to
- * 3 bytes a value in a buffer of
+ * a B of 128 MiB to 1 GiB (or as a tuned shape says) a call first rounds B
+ * to TF32 and packs each row to 3 bytes a value in a buffer of about
  * 3 cols K bytes from the library's memory pool (released in stream order):
- * the SpMM then gathers a quarter fewer bytes, with bit-identical results. */
+ * the SpMM then gathers a quarter fewer bytes, with bit-identical results.
+ * ACCSPMM_PACK=0 in the environment turns this off. */
 int accspmm_spmm_tf32(const accspmm_metcf_t* metcf, const float* B, float* C,
                       uint32_t K, int32_t precision, void* stream);
 
@@ -369,7 +370,9 @@ int accspmm_gather_floor(const accspmm_metcf_t* metcf, const float* B, uint32_t 
  * shapes -- kernel variant (register-direct at 3 or 2 CTAs per SM, with or
  * without the rolling tile ring that keeps gathers in flight through the
  * MMAs; double-buffered), feature-slice width (32/64/128 columns) and windows
- * per CTA (4/8/16/32, the load-balance granularity) -- on this matrix with this B, and keeps the fastest for the
+ * per CTA (4/8/16/32, the load-balance granularity), and for TF32 at
+ * 128-column slices with the ring B read directly or packed -- on this matrix
+ * with this B, and keeps the fastest for the
  * matrix's signature (windows, tiles, K, precision) for the rest of the
  * process: later plain, adaptive and batched calls on a matrix with that
  * signature use it.  C is overwritten.  Results of different shapes agree
@@ -384,6 +387,7 @@ typedef struct accspmm_tune_result {
     uint32_t candidates;
     uint32_t ctas_per_sm;      /* resident CTAs per SM of the chosen kernel */
     int32_t tile_ring;         /* rolling tile ring: 1 on, 0 off, -1 the default rule */
+    int32_t packed_b;          /* gathers from a packed TF32 copy of B: 1 on, 0 off, -1 the default rule */
 } accspmm_tune_result_t;
 
 int accspmm_autotune_metcf(const accspmm_metcf_t* metcf, const float* B, float* C,

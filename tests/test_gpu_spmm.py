@@ -282,12 +282,13 @@ def test_tf32_rounding_is_rna_bit_exact():
     np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
 
 
-def test_autotune_picks_a_shape_that_is_used_and_correct():
+@pytest.mark.parametrize("K", [64, 128])
+def test_autotune_picks_a_shape_that_is_used_and_correct(K):
+    """At K = 128 the candidates include gathering from a packed B."""
     g = gold("plsym1000")
     csr = csr_of_gold(g)
     m = device_metcf(csr)
     h = m.to_numpy()
-    K = 64
     B = np.random.default_rng(8).uniform(-1, 1, (csr["cols"], K)).astype(np.float32)
     dB = torch_dev(B)
     dC = empty_dev(m.c_rows, K)
@@ -296,6 +297,7 @@ def test_autotune_picks_a_shape_that_is_used_and_correct():
         # the default shape is one of the candidates and may win
         assert r["slice_width"] in (32, 64, 128) and r["windows_per_cta"] >= 1
         assert r["candidates"] > 1 and r["best_ms"] <= r["default_ms"] + 1e-6
+        assert r["packed_b"] in (-1, 0, 1)
         got = spmm_plain(m, B, K)
         c64 = oracle.spmm_metcf_f64(h, csr["cols"], B)
         assert rel_fro(got, c64) < TOL_TF32_VS_F64
@@ -578,11 +580,11 @@ def test_device_builders_match_the_oracle_at_full_size():
 
 @pytest.mark.parametrize("K", [136, 256])
 def test_packed_b_is_bit_identical(monkeypatch, K):
-    """TF32 launches at 128-column slices whose B is at least 128 MiB first
-    pack B to 3 bytes a value (rounded to TF32 and split in two planes); the
-    SpMM on the packed planes returns bitwise what the kernel reading B
-    directly returns, on the plain and adaptive entry points, within the TF32
-    tolerance of FP64 on sampled rows."""
+    """TF32 launches at 128-column slices whose B is 128 MiB to 1 GiB first
+    pack B to 3 bytes a value (rounded to TF32; each row its upper halfwords,
+    then its third bytes); the SpMM on the packed copy returns bitwise what
+    the kernel reading B directly returns, on the plain and adaptive entry
+    points, within the TF32 tolerance of FP64 on sampled rows."""
     n = 1 << 18
     rp, ci, vals = synth.powerlaw_local(n=n, seed=4)
     csr = dict(rows=n, cols=n, nnz=len(ci), row_ptr=rp, col_idx=ci, data=vals)
@@ -606,3 +608,29 @@ def test_packed_b_is_bit_identical(monkeypatch, K):
     ref = oracle.spmm_csr_f64(sub_rp, sub_ci, sub_v, dB.cpu().numpy())
     got = out["1"][0][torch.from_numpy(rows).cuda()].cpu().numpy()
     assert rel_fro(got, ref) < TOL_TF32_VS_F64
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("K", [72, 128, 200])
+def test_forced_packing_on_a_small_b_is_bit_identical(monkeypatch, K):
+    """ACCSPMM_PACK=2 packs B wherever the launch shape allows, also below the
+    default rule's 128 MiB: ragged last slices (K = 72, 200), rows that are
+    not a multiple of the window height, the plain and adaptive entry points."""
+    n = 5003
+    rp, ci, vals = synth.powerlaw_local(n=n, seed=7)
+    csr = dict(rows=n, cols=n, nnz=len(ci), row_ptr=rp, col_idx=ci, data=vals)
+    m = device_metcf(csr)
+    a = m.adpbme()
+    cr = a.c_rows()
+    dB = torch.rand((n, K), device="cuda") * 2 - 1
+    out = {}
+    for pk in ("2", "0"):
+        monkeypatch.setenv("ACCSPMM_PACK", pk)
+        C, Ca = empty_dev(m.c_rows, K), empty_dev(cr, K)
+        m.spmm(dB, C, K)
+        a.spmm(dB, Ca, cr, K)
+        torch.cuda.synchronize()
+        out[pk] = (C, Ca)
+    assert torch.equal(out["2"][0], out["0"][0]) and torch.equal(out["2"][1], out["0"][1])
+    ref = oracle.spmm_csr_f64(rp, ci, vals, dB.cpu().numpy())
+    assert rel_fro(out["2"][0][:n].cpu().numpy(), ref) < TOL_TF32_VS_F64
