@@ -72,11 +72,14 @@ __global__ void __launch_bounds__(NW * 32, MINB) spmm_window_packed_kernel(const
 }
 
 // B rounded to TF32 (cvt.rna, as the SpMM's operands are) and packed row by
-// row: K halfwords of bits 31..16, then K bytes of bits 15..8, which hold
-// every set bit of the rounded value above bit 12 -- 3 bytes a value, a row
-// one contiguous run of `pitch` bytes (3K rounded up to 16), so that a
-// gathered row stays in one DRAM page.  One float4 of B per thread and step,
-// read once with a streaming load.
+// row: K halfwords of bits 31..16, then per 128-column slice 64 bytes that
+// hold bits 15..12 of two values each (the even value in the high nibble),
+// ordered so that the 16 values one lane of the SpMM takes from a slice
+// (column group g: values 32h + 4g + 0..3, h = 0..3) have their nibbles in 8
+// adjacent bytes -- every bit the tensor core reads (31..13) in 2.5 bytes a
+// value, a row one contiguous run of `pitch` bytes (2K + 64 per slice,
+// rounded up to 16), so that a gathered row stays in one DRAM page.  One
+// float4 of B per thread and step, read once with a streaming load.
 __global__ void pack_tf32_kernel(const float4* __restrict__ B, uint8_t* __restrict__ P, uint32_t K,
                                  uint32_t pitch, size_t n4) {
     const uint32_t k4 = K / 4;
@@ -89,9 +92,10 @@ __global__ void pack_tf32_kernel(const float4* __restrict__ B, uint8_t* __restri
         uint8_t* base = P + row * pitch;
         *reinterpret_cast<uint2*>(base + 2 * c) =
             make_uint2((r0 >> 16) | (r1 & 0xFFFF0000u), (r2 >> 16) | (r3 & 0xFFFF0000u));
-        *reinterpret_cast<uint32_t*>(base + 2 * K + c) =
-            ((r0 >> 8) & 0xFFu) | (((r1 >> 8) & 0xFFu) << 8) | (((r2 >> 8) & 0xFFu) << 16) |
-            (((r3 >> 8) & 0xFFu) << 24);
+        // nibbles of values c .. c + 3: slice c / 128, column group (c / 4) % 8, h = (c / 32) % 4
+        *reinterpret_cast<uint16_t*>(base + 2 * K + 64 * (c >> 7) + 8 * ((c >> 2) & 7) + 2 * ((c >> 5) & 3)) =
+            uint16_t(((r0 >> 8) & 0xF0u) | ((r1 >> 12) & 0x0Fu) | (((r2 >> 8) & 0xF0u) << 8) |
+                     (((r3 >> 12) & 0x0Fu) << 8));
     }
 }
 
@@ -641,27 +645,24 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     const bool x3 = precision == ACCSPMM_PREC_3XTF32;
     const int occ = cfg.occ;
     // TF32 at 128-column slices with the ring: B is first rounded to TF32 and
-    // packed to 3 bytes a value (pack_tf32_kernel), so the SpMM gathers 12 of
-    // every 16 sectors of a row; the MMAs see the same operand bits, so the
-    // results are bit-identical.  On the 1M-row power-law matrix: 2.18 ms per
-    // call (packing included) against 2.30 ms at K = 128, 4.27 against 4.45 ms
-    // at K = 256.  The default rule packs a B of 128 MiB to 1 GiB: at 64-column
-    // slices (K = 64) the packing pass cost what the gathers saved; a B that
-    // fits the L2 (the 16,384-row matrix, 53.5 against 52.0 us) only gains a
-    // pass; and the larger the B against the L2, the less of the gain from
-    // holding more rows there is left while the pass (7 bytes a value) grows:
-    // on the 2M-row GCN graph at K = 256 (a 2 GiB B) the packed call took
-    // 7.61 ms against 7.46.  The autotuner times both ways.
+    // packed to 2.5 bytes a value (pack_tf32_kernel), so the SpMM gathers 10
+    // of every 16 sectors of a row; the MMAs see the same operand bits, so
+    // the results are bit-identical.  On the 1M-row power-law matrix: 2.02 ms
+    // per call (packing included) against 2.30 ms at K = 128, 3.98 against
+    // 4.45 ms at K = 256; on the 2M-row GCN graph at K = 256 (a 2 GiB B) 7.13
+    // against 7.47 ms.  The default rule packs a B of at least 128 MiB: at
+    // 64-column slices (K = 64) a 3-byte packing cost what the gathers saved,
+    // and a B that fits the L2 (the 16,384-row matrix, 53.5 against 52.0 us)
+    // only gains a pass.  The autotuner times both ways.
     const int roll = env_int("ACCSPMM_ROLL", cfg.ring);
     const bool ring_on = roll < 0 || roll != 0;
     const uint64_t b_bytes = uint64_t(cols) * K * 4;
-    const bool pack_rule = cfg.pack > 0 ||
-                           (cfg.pack < 0 && b_bytes >= (uint64_t(128) << 20) && b_bytes <= (uint64_t(1) << 30));
+    const bool pack_rule = cfg.pack > 0 || (cfg.pack < 0 && b_bytes >= (uint64_t(128) << 20));
     if (allow_pack && !x3 && !(epi.bias || epi.act) && ring_on && cfg.fs == 128 && occ == 2 && pack_rule) {
         cudaMemPool_t pool;
         int st = library_pool(&pool);
         if (st) return st;
-        const uint32_t pitch = (3 * K + 15) / 16 * 16;
+        const uint32_t pitch = (2 * K + 64 * ((K + 127) / 128) + 15) / 16 * 16;
         void* packed = nullptr;
         ACC_CUDA(cudaMallocFromPoolAsync(&packed, size_t(cols) * pitch + 64, pool, s));
         a.bp = static_cast<const uint8_t*>(packed);

@@ -90,30 +90,32 @@ __device__ __forceinline__ float comp(const float4& v, int j) {
 
 // Four packed TF32 values of one row of B: halfwords (bits 31..16) in hi,
 // bytes (bits 15..8) in lo.
-struct Packed4 {
-    uint2 hi;
-    uint32_t lo;
-};
-
-__device__ __forceinline__ Packed4 ldg_packed4_ordered(const uint8_t* h, const uint8_t* l) {
-    Packed4 v;
-    asm volatile("ld.global.nc.v2.u32 {%0, %1}, [%2];" : "=r"(v.hi.x), "=r"(v.hi.y) : "l"(h));
-    asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(v.lo) : "l"(l));
+// Packed TF32 B at 128-column slices (pack_tf32_kernel).  For one gathered
+// row a lane of column group g holds hw[h] = bits 31..16 of values
+// 32h + 4g + 0..3 (two to a word, h = 0..3) and nb = 8 nibble bytes: byte
+// 2h + (j >> 1) holds bits 15..12 of value 32h + 4g + j, even j in the high
+// nibble.  Word hp of nb covers h = 2hp and 2hp + 1.
+__device__ __forceinline__ uint2 ldg_u2_ordered(const uint8_t* p) {
+    uint2 v;
+    asm volatile("ld.global.nc.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
     return v;
 }
 
-// The 32-bit TF32 operand of value j of a Packed4: one byte permute puts
-// halfword j in bits 31..16 and byte j in bits 15..8; bits 7..0 take any
-// byte, and the tensor core reads only bits 31..13, which equal the value's
-// cvt.rna rounding (the packing stored them).
-template <int J>
-__device__ __forceinline__ uint32_t unpack_tf32(const Packed4& v) {
-    constexpr uint32_t lo_b = 4 + J;                 // byte J of the second source
+// The 32-bit TF32 operand of value j of column group h (HB = h & 1): one
+// byte permute puts its halfword in bits 31..16 and the nibble byte that
+// holds its bits 15..12 in bits 15..8, its nibble on top (for odd j from the
+// nibble word shifted up by four bits).  Bits 11..0 take whatever comes along,
+// and the tensor core reads only bits 31..13, which equal the value's cvt.rna
+// rounding (the packing stored them).
+template <int J, int HB>
+__device__ __forceinline__ uint32_t unpack_tf32(uint2 hw, uint32_t nbw, uint32_t nbw_shl4) {
+    constexpr uint32_t lo_b = 4 + 2 * HB + (J >> 1);  // byte of the second source
     constexpr uint32_t hi_b0 = 2 * (J & 1), hi_b1 = hi_b0 + 1;
     constexpr uint32_t sel = 0u | (lo_b << 4) | (hi_b0 << 8) | (hi_b1 << 12);
-    const uint32_t hw = J < 2 ? v.hi.x : v.hi.y;
+    const uint32_t w = J < 2 ? hw.x : hw.y;
+    const uint32_t nb = (J & 1) ? nbw_shl4 : nbw;
     uint32_t r;
-    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(hw), "r"(v.lo), "n"(sel));
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(w), "r"(nb), "n"(sel));
     return r;
 }
 
@@ -194,33 +196,29 @@ __device__ __forceinline__ void tile_mma(float (&acc)[Layout<H>::NM][4], const f
 }
 
 // tile_mma for TF32 with B already rounded and packed: the same MMAs on the
-// same operand bits (element j of float4 h of a row is value j of Packed4 h).
+// same operand bits (element j of float4 h of a row is value j of column
+// group h of the packed row).
 template <int H>
-__device__ __forceinline__ void tile_mma_packed(float (&acc)[Layout<H>::NM][4], const Packed4 (&r0)[H],
-                                                const Packed4 (&r1)[H], float av0, float av1) {
+__device__ __forceinline__ void tile_mma_packed(float (&acc)[Layout<H>::NM][4], const uint2 (&h0)[H], uint2 n0,
+                                                const uint2 (&h1)[H], uint2 n1, float av0, float av1) {
+    static_assert(H == 4, "packed B is gathered at 128-column slices");
     constexpr int NM = Layout<H>::NM;
     const uint32_t b0 = f2tf32(av0), b1 = f2tf32(av1);
+    const uint32_t n0s[2] = {n0.x << 4, n0.y << 4}, n1s[2] = {n1.x << 4, n1.y << 4};
+    const uint32_t n0w[2] = {n0.x, n0.y}, n1w[2] = {n1.x, n1.y};
 #pragma unroll
     for (int m = 0; m < NM; ++m) {
+        const int hp = m >> 2, j = m & 3;
         uint32_t x0, x1, x2, x3;
-        if constexpr (H >= 2) {
-            const int hp = m >> 2, j = m & 3;
-#define ACC_PK(J)                                                     \
-    if (j == J) {                                                     \
-        x0 = unpack_tf32<J>(r0[2 * hp]); x1 = unpack_tf32<J>(r0[2 * hp + 1]); \
-        x2 = unpack_tf32<J>(r1[2 * hp]); x3 = unpack_tf32<J>(r1[2 * hp + 1]); \
+#define ACC_PK(J)                                                                                \
+    if (j == J) {                                                                                \
+        x0 = unpack_tf32<J, 0>(h0[2 * hp], n0w[hp], n0s[hp]);                                    \
+        x1 = unpack_tf32<J, 1>(h0[2 * hp + 1], n0w[hp], n0s[hp]);                                \
+        x2 = unpack_tf32<J, 0>(h1[2 * hp], n1w[hp], n1s[hp]);                                    \
+        x3 = unpack_tf32<J, 1>(h1[2 * hp + 1], n1w[hp], n1s[hp]);                                \
     }
-            ACC_PK(0) ACC_PK(1) ACC_PK(2) ACC_PK(3)
+        ACC_PK(0) ACC_PK(1) ACC_PK(2) ACC_PK(3)
 #undef ACC_PK
-        } else {
-            if (m == 0) {
-                x0 = unpack_tf32<0>(r0[0]); x1 = unpack_tf32<2>(r0[0]);
-                x2 = unpack_tf32<0>(r1[0]); x3 = unpack_tf32<2>(r1[0]);
-            } else {
-                x0 = unpack_tf32<1>(r0[0]); x1 = unpack_tf32<3>(r0[0]);
-                x2 = unpack_tf32<1>(r1[0]); x3 = unpack_tf32<3>(r1[0]);
-            }
-        }
         mma_tf32(acc[m], x0, x1, x2, x3, b0, b1);
     }
 }

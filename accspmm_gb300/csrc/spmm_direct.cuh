@@ -209,11 +209,13 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
 
         BitDecode dec;
         dec.init(g, tq);
-        // this lane's first value of a row: halfword f0 + 4g, byte 2K + f0 + 4g
+        // this lane's halfwords of a row start at byte 2 (f0 + 4g), its 8
+        // nibble bytes at 2K + 64 (f0 / 128) + 8g
         const uint8_t* Pl = a.bp + 2 * (blk.f0 + 4 * g);
-        const size_t lo_off = size_t(2) * a.K - (blk.f0 + 4 * g);
+        const ptrdiff_t nb_off = ptrdiff_t(2) * a.K + ptrdiff_t(blk.f0 / 128) * 64 + 8 * g -
+                                 ptrdiff_t(2) * (blk.f0 + 4 * g);
         float av0[U], av1[U];
-        Packed4 r0[U][H], r1[U][H];
+        uint2 h0[U][H], h1[U][H], n0[U], n1[U];
         auto issue = [&](int u) {
             const uint32_t i0 = __shfl_sync(0xffffffffu, ma[(8 * u) / 32], (8 * u + tq) & 31);
             const uint32_t i1 = __shfl_sync(0xffffffffu, ma[(8 * u) / 32], (8 * u + tq + 4) & 31);
@@ -227,13 +229,16 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
             const bool v0 = i0 < a.cols, v1 = i1 < a.cols;
             const uint8_t* w0 = Pl + size_t(v0 ? i0 : 0) * a.bpitch;
             const uint8_t* w1 = Pl + size_t(v1 ? i1 : 0) * a.bpitch;
+            const uint2 zero = make_uint2(0u, 0u);
 #pragma unroll
             for (int h = 0; h < H; ++h) {
-                const Packed4 zero{make_uint2(0u, 0u), 0u};
-                // halfwords at w + 64 h, bytes at w + lo_off + 32 h
-                r0[u][h] = (v0 && fok[h]) ? ldg_packed4_ordered(w0 + 64 * h, w0 + lo_off + 32 * h) : zero;
-                r1[u][h] = (v1 && fok[h]) ? ldg_packed4_ordered(w1 + 64 * h, w1 + lo_off + 32 * h) : zero;
+                // halfwords of values 32h + 4g + 0..3 at w + 64 h
+                h0[u][h] = (v0 && fok[h]) ? ldg_u2_ordered(w0 + 64 * h) : zero;
+                h1[u][h] = (v1 && fok[h]) ? ldg_u2_ordered(w1 + 64 * h) : zero;
             }
+            // nibbles of all 16 values in one load (fok[0] holds whenever any fok[h] does)
+            n0[u] = (v0 && fok[0]) ? ldg_u2_ordered(w0 + nb_off) : zero;
+            n1[u] = (v1 && fok[0]) ? ldg_u2_ordered(w1 + nb_off) : zero;
         };
 #pragma unroll
         for (int u = 0; u < U; ++u) issue(u);
@@ -251,7 +256,7 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
                         while (blk.s_rwo[wl + 1] <= tt) ++wl;
                         next_bound = blk.s_rwo[wl + 1];
                     }
-                    tile_mma_packed<H>(acc, r0[u], r1[u], av0[u], av1[u]);
+                    tile_mma_packed<H>(acc, h0[u], n0[u], h1[u], n1[u], av0[u], av1[u]);
                 }
                 issue(u);  // tile t + U + u
             }

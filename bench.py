@@ -448,11 +448,11 @@ def run_ours(args):
             m.spmm(Bt, Ct, K, prec, stream)
 
     # per step: the SpMM launch, preceded for TF32 at 128-column slices
-    # (K > 64) with a B of 128 MiB to 1 GiB (the library's default rule, or
+    # (K > 64) with a B of at least 128 MiB (the library's default rule, or
     # as the tuned shape says) by the launch that packs B to TF32; the
     # adaptive path's window offsets are derived once per AdpBME (during the
     # warm-up) and kept
-    pack_rule = K > 64 and (128 << 20) <= n * K * 4 <= (1 << 30)
+    pack_rule = K > 64 and n * K * 4 >= (128 << 20)
     if tune is not None and tune["packed_b"] >= 0:
         pack_rule = tune["packed_b"] == 1
     launches_per_step = 2 if (prec == capi.PREC_TF32 and pack_rule
