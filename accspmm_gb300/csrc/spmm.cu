@@ -72,14 +72,15 @@ __global__ void __launch_bounds__(NW * 32, MINB) spmm_window_packed_kernel(const
 }
 
 // B rounded to TF32 (cvt.rna, as the SpMM's operands are) and packed row by
-// row: K halfwords of bits 31..16, then per 128-column slice 64 bytes that
-// hold bits 15..12 of two values each (the even value in the high nibble),
-// ordered so that the 16 values one lane of the SpMM takes from a slice
-// (column group g: values 32h + 4g + 0..3, h = 0..3) have their nibbles in 8
-// adjacent bytes -- every bit the tensor core reads (31..13) in 2.5 bytes a
-// value, a row one contiguous run of `pitch` bytes (2K + 64 per slice,
-// rounded up to 16), so that a gathered row stays in one DRAM page.  One
-// float4 of B per thread and step, read once with a streaming load.
+// row, 320 bytes per 128-column slice (`pitch` = 320 x slices, the last
+// slice padded): every bit the tensor core reads (31..13) in 2.5 bytes a
+// value, a gathered row one contiguous run in one DRAM page.  In a slice the
+// SpMM lane of column group g takes values 32h + 4g + 0..3 (h = 0..3): their
+// halfwords of bits 31..16 for h = 2hp, 2hp + 1 are 16 adjacent bytes at
+// 128 hp + 16 g (one 16-byte load each), and bits 15..12 of all 16 values
+// are 8 adjacent nibble bytes at 256 + 8 g (one 8-byte load), byte 2h + j / 2
+// holding value j's bits in its high nibble for even j, low nibble for odd.
+// One float4 of B per thread and step, read once with a streaming load.
 __global__ void pack_tf32_kernel(const float4* __restrict__ B, uint8_t* __restrict__ P, uint32_t K,
                                  uint32_t pitch, size_t n4) {
     const uint32_t k4 = K / 4;
@@ -89,11 +90,12 @@ __global__ void pack_tf32_kernel(const float4* __restrict__ B, uint8_t* __restri
         const uint32_t c = uint32_t(i - row * k4) * 4;
         const float4 v = __ldcs(B + i);
         const uint32_t r0 = f2tf32(v.x), r1 = f2tf32(v.y), r2 = f2tf32(v.z), r3 = f2tf32(v.w);
-        uint8_t* base = P + row * pitch;
-        *reinterpret_cast<uint2*>(base + 2 * c) =
+        // slice c / 128 of the row: column group g = (c / 4) % 8, h = (c / 32) % 4
+        uint8_t* base = P + row * pitch + 320 * (c >> 7);
+        const uint32_t g = (c >> 2) & 7, h = (c >> 5) & 3;
+        *reinterpret_cast<uint2*>(base + 128 * (h >> 1) + 16 * g + 8 * (h & 1)) =
             make_uint2((r0 >> 16) | (r1 & 0xFFFF0000u), (r2 >> 16) | (r3 & 0xFFFF0000u));
-        // nibbles of values c .. c + 3: slice c / 128, column group (c / 4) % 8, h = (c / 32) % 4
-        *reinterpret_cast<uint16_t*>(base + 2 * K + 64 * (c >> 7) + 8 * ((c >> 2) & 7) + 2 * ((c >> 5) & 3)) =
+        *reinterpret_cast<uint16_t*>(base + 256 + 8 * g + 2 * h) =
             uint16_t(((r0 >> 8) & 0xF0u) | ((r1 >> 12) & 0x0Fu) | (((r2 >> 8) & 0xF0u) << 8) |
                      (((r3 >> 12) & 0x0Fu) << 8));
     }
@@ -646,11 +648,11 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     const int occ = cfg.occ;
     // TF32 at 128-column slices with the ring: B is first rounded to TF32 and
     // packed to 2.5 bytes a value (pack_tf32_kernel), so the SpMM gathers 10
-    // of every 16 sectors of a row; the MMAs see the same operand bits, so
-    // the results are bit-identical.  On the 1M-row power-law matrix: 2.02 ms
-    // per call (packing included) against 2.30 ms at K = 128, 3.98 against
-    // 4.45 ms at K = 256; on the 2M-row GCN graph at K = 256 (a 2 GiB B) 7.13
-    // against 7.47 ms.  The default rule packs a B of at least 128 MiB: at
+    // of every 16 sectors of a row in 3 instead of 4 loads; the MMAs see the
+    // same operand bits, so the results are bit-identical.  On the 1M-row
+    // power-law matrix: 2.00 ms per call (packing included) against 2.30 ms
+    // at K = 128, 3.91 against 4.45 ms at K = 256; on the 2M-row GCN graph at
+    // K = 256 (a 2 GiB B) 6.95 against 7.46 ms.  The default rule packs a B of at least 128 MiB: at
     // 64-column slices (K = 64) a 3-byte packing cost what the gathers saved,
     // and a B that fits the L2 (the 16,384-row matrix, 53.5 against 52.0 us)
     // only gains a pass.  The autotuner times both ways.
@@ -662,7 +664,7 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
         cudaMemPool_t pool;
         int st = library_pool(&pool);
         if (st) return st;
-        const uint32_t pitch = (2 * K + 64 * ((K + 127) / 128) + 15) / 16 * 16;
+        const uint32_t pitch = 320 * ((K + 127) / 128);
         void* packed = nullptr;
         ACC_CUDA(cudaMallocFromPoolAsync(&packed, size_t(cols) * pitch + 64, pool, s));
         a.bp = static_cast<const uint8_t*>(packed);

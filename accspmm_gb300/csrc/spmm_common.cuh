@@ -95,6 +95,14 @@ __device__ __forceinline__ float comp(const float4& v, int j) {
 // 32h + 4g + 0..3 (two to a word, h = 0..3) and nb = 8 nibble bytes: byte
 // 2h + (j >> 1) holds bits 15..12 of value 32h + 4g + j, even j in the high
 // nibble.  Word hp of nb covers h = 2hp and 2hp + 1.
+__device__ __forceinline__ uint4 ldg_u4_ordered(const uint8_t* p) {
+    uint4 v;
+    asm volatile("ld.global.nc.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p));
+    return v;
+}
+
 __device__ __forceinline__ uint2 ldg_u2_ordered(const uint8_t* p) {
     uint2 v;
     asm volatile("ld.global.nc.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));

@@ -209,11 +209,11 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
 
         BitDecode dec;
         dec.init(g, tq);
-        // this lane's halfwords of a row start at byte 2 (f0 + 4g), its 8
-        // nibble bytes at 2K + 64 (f0 / 128) + 8g
-        const uint8_t* Pl = a.bp + 2 * (blk.f0 + 4 * g);
-        const ptrdiff_t nb_off = ptrdiff_t(2) * a.K + ptrdiff_t(blk.f0 / 128) * 64 + 8 * g -
-                                 ptrdiff_t(2) * (blk.f0 + 4 * g);
+        // a row's slice f0 / 128 is 320 bytes at 320 (f0 / 128): this lane's
+        // halfwords of column groups h = 2hp, 2hp + 1 at 128 hp + 16 g, its 8
+        // nibble bytes at 256 + 8g
+        const uint8_t* Pl = a.bp + 320 * (blk.f0 / 128) + 16 * g;
+        const int nb_off = 256 - 8 * g;
         float av0[U], av1[U];
         uint2 h0[U][H], h1[U][H], n0[U], n1[U];
         auto issue = [&](int u) {
@@ -231,10 +231,15 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
             const uint8_t* w1 = Pl + size_t(v1 ? i1 : 0) * a.bpitch;
             const uint2 zero = make_uint2(0u, 0u);
 #pragma unroll
-            for (int h = 0; h < H; ++h) {
-                // halfwords of values 32h + 4g + 0..3 at w + 64 h
-                h0[u][h] = (v0 && fok[h]) ? ldg_u2_ordered(w0 + 64 * h) : zero;
-                h1[u][h] = (v1 && fok[h]) ? ldg_u2_ordered(w1 + 64 * h) : zero;
+            for (int hp = 0; hp < H / 2; ++hp) {
+                // halfwords of values 32h + 4g + 0..3, h = 2hp and 2hp + 1, at w + 128 hp
+                const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
+                const uint4 p0 = (v0 && fok[2 * hp]) ? ldg_u4_ordered(w0 + 128 * hp) : z4;
+                const uint4 p1 = (v1 && fok[2 * hp]) ? ldg_u4_ordered(w1 + 128 * hp) : z4;
+                h0[u][2 * hp] = make_uint2(p0.x, p0.y);
+                h1[u][2 * hp] = make_uint2(p1.x, p1.y);
+                h0[u][2 * hp + 1] = fok[2 * hp + 1] ? make_uint2(p0.z, p0.w) : zero;
+                h1[u][2 * hp + 1] = fok[2 * hp + 1] ? make_uint2(p1.z, p1.w) : zero;
             }
             // nibbles of all 16 values in one load (fok[0] holds whenever any fok[h] does)
             n0[u] = (v0 && fok[0]) ? ldg_u2_ordered(w0 + nb_off) : zero;

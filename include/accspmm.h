@@ -245,10 +245,10 @@ void accspmm_adpbme_destroy(accspmm_adpbme_t* adp);
  * Calls may be captured into a CUDA graph; a call captured before the
  * schedule exists runs the blocks in window order.  In TF32 with K > 64 and
  * a B of at least 128 MiB (or as a tuned shape says) a call first rounds B
- * to TF32 and packs each row to 2.5 bytes a value in a buffer of about
- * 2.5 cols K bytes from the library's memory pool (released in stream
- * order): the SpMM then gathers 10 instead of 16 sectors of each 128-column
- * row slice, with bit-identical results.
+ * to TF32 and packs each row to 2.5 bytes a value in a buffer of
+ * 320 cols ceil(K / 128) bytes from the library's memory pool (released in
+ * stream order): the SpMM then gathers 10 instead of 16 sectors of each
+ * 128-column row slice, with bit-identical results.
  * ACCSPMM_PACK=0 in the environment turns this off. */
 int accspmm_spmm_tf32(const accspmm_metcf_t* metcf, const float* B, float* C,
                       uint32_t K, int32_t precision, void* stream);
