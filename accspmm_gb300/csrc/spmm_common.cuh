@@ -88,8 +88,6 @@ __device__ __forceinline__ float comp(const float4& v, int j) {
     return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w;
 }
 
-// Four packed TF32 values of one row of B: halfwords (bits 31..16) in hi,
-// bytes (bits 15..8) in lo.
 // Packed TF32 B at 128-column slices (pack_tf32_kernel).  For one gathered
 // row a lane of column group g holds hw[h] = bits 31..16 of values
 // 32h + 4g + 0..3 (two to a word, h = 0..3) and nb = 8 nibble bytes: byte
