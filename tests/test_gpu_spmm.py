@@ -580,9 +580,10 @@ def test_device_builders_match_the_oracle_at_full_size():
 
 @pytest.mark.parametrize("K", [136, 256])
 def test_packed_b_is_bit_identical(monkeypatch, K):
-    """TF32 launches at 128-column slices whose B is 128 MiB to 1 GiB first
-    pack B to 3 bytes a value (rounded to TF32; each row its upper halfwords,
-    then its third bytes); the SpMM on the packed copy returns bitwise what
+    """TF32 launches at 128-column slices whose B is at least 128 MiB first
+    pack B to 2.5 bytes a value (rounded to TF32; each 128-column slice of a
+    row its halfwords of bits 31..16, then the nibbles of bits 15..12); the
+    SpMM on the packed copy returns bitwise what
     the kernel reading B directly returns, on the plain and adaptive entry
     points, within the TF32 tolerance of FP64 on sampled rows."""
     n = 1 << 18
