@@ -165,10 +165,14 @@ __device__ __forceinline__ void direct_item(const SpmmArgs& a, const Block<FS, N
 
 
 // direct_item with the rolling tile ring for TF32 with B packed (a.bp, rows
-// of a.bpitch bytes: three bytes a value instead of four, so 12 of every 16
+// of a.bpitch bytes: 2.5 bytes a value instead of four, so 10 of every 16
 // sectors of a gathered row).  Same pieces, same MMAs on the same operand bits, same
 // order: bit-identical to direct_item<FS, TF32, U, false, NW, true>.
-template <int FS, int U, int NW = kDirectNW>
+// PF: the B rows of the tile group two ahead of the one being loaded are
+// prefetched into L2 (one bulk prefetch of the row's 320-byte slice per
+// sparseA2B entry), so that the ring's loads of them find L2 instead of DRAM;
+// a hint only, it changes no value.
+template <int FS, int U, int NW = kDirectNW, bool PF = false>
 __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Block<FS, NW>& blk) {
     constexpr int H = FS / 32;
     using L = Layout<H>;
@@ -245,9 +249,25 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
             n0[u] = (v0 && fok[0]) ? ldg_u2_ordered(w0 + nb_off) : zero;
             n1[u] = (v1 && fok[0]) ? ldg_u2_ordered(w1 + nb_off) : zero;
         };
+        // PF: sparseA2B entry `lane` of the group two ahead of the issue group
+        static_assert(!PF || 8 * U <= 32, "one prefetched row per lane");
+        uint32_t mp = kPad;
+        auto load_pf = [&](uint32_t t) {
+            if (PF) {
+                const uint32_t tile = t + uint32_t(lane) / 8;
+                mp = (lane < 8 * U && tile < te) ? __ldg(a.a2b + size_t(t) * 8 + lane) : kPad;
+            }
+        };
+        auto prefetch_rows = [&]() {
+            if (PF && mp < a.cols) {
+                const uint8_t* r = a.bp + size_t(mp) * a.bpitch + 320 * (blk.f0 / 128);
+                asm volatile("cp.async.bulk.prefetch.L2.global [%0], 320;" ::"l"(r) : "memory");
+            }
+        };
 #pragma unroll
         for (int u = 0; u < U; ++u) issue(u);
         load_meta(tb + U);  // padding when past te
+        load_pf(tb + 2 * U);
         for (uint32_t t = tb; t < te; t += U) {
 #pragma unroll
             for (int u = 0; u < U; ++u) {
@@ -264,8 +284,10 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
                     tile_mma_packed<H>(acc, h0[u], n0[u], h1[u], n1[u], av0[u], av1[u]);
                 }
                 issue(u);  // tile t + U + u
+                if (u == 0) prefetch_rows();  // tiles t + 2U .. t + 3U - 1
             }
             load_meta(t + 2 * U);
+            load_pf(t + 3 * U);
         }
         blk.template flush<false>(a, acc, wl, tb, te, first_win);
     }

@@ -248,8 +248,10 @@ void accspmm_adpbme_destroy(accspmm_adpbme_t* adp);
  * to TF32 and packs each row to 2.5 bytes a value in a buffer of
  * 320 cols ceil(K / 128) bytes from the library's memory pool (released in
  * stream order): the SpMM then gathers 10 instead of 16 sectors of each
- * 128-column row slice, with bit-identical results.
- * ACCSPMM_PACK=0 in the environment turns this off. */
+ * 128-column row slice, with bit-identical results, and prefetches into L2
+ * the rows of the tile group two ahead of the one it loads.
+ * ACCSPMM_PACK=0 in the environment turns the packing off,
+ * ACCSPMM_PREFETCH=0 the prefetch. */
 int accspmm_spmm_tf32(const accspmm_metcf_t* metcf, const float* B, float* C,
                       uint32_t K, int32_t precision, void* stream);
 

@@ -578,6 +578,34 @@ def test_device_builders_match_the_oracle_at_full_size():
         np.testing.assert_array_equal(a[k], o[k], err_msg=k)
 
 
+@pytest.mark.slow
+def test_packed_b_with_prefetch_is_bit_identical_at_full_size(monkeypatch):
+    """On the 1M-row power-law matrix (seed 0, K = 128, a 512 MB B) the packed
+    kernel returns the same bits with its L2 prefetch of the rows two tile
+    groups ahead (the default), without it (ACCSPMM_PREFETCH=0), and reading
+    fp32 B directly (ACCSPMM_PACK=0), on the plain and adaptive entry points."""
+    n, K = 1 << 20, 128
+    rp, ci, vals = synth.powerlaw_local(n=n, seed=0)
+    csr = dict(rows=n, cols=n, nnz=len(ci), row_ptr=rp, col_idx=ci, data=vals)
+    m = device_metcf(csr)
+    a = m.adpbme()
+    cr = a.c_rows()
+    dB = torch.rand((n, K), device="cuda", generator=torch.Generator(device="cuda").manual_seed(0)) * 2 - 1
+    out = {}
+    for pf, pk in (("1", "1"), ("0", "1"), ("1", "0")):
+        monkeypatch.setenv("ACCSPMM_PREFETCH", pf)
+        monkeypatch.setenv("ACCSPMM_PACK", pk)
+        C, Ca = empty_dev(m.c_rows, K), empty_dev(cr, K)
+        m.spmm(dB, C, K)
+        a.spmm(dB, Ca, cr, K)
+        torch.cuda.synchronize()
+        out[pf + pk] = (C, Ca)
+    for key in ("01", "10"):
+        assert torch.equal(out["11"][0], out[key][0]), key
+        assert torch.equal(out["11"][1], out[key][1]), key
+    assert torch.isfinite(out["11"][0]).all()
+
+
 @pytest.mark.parametrize("K", [136, 256])
 def test_packed_b_is_bit_identical(monkeypatch, K):
     """TF32 launches at 128-column slices whose B is at least 128 MiB first
