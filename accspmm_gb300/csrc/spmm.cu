@@ -677,8 +677,8 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
             st = cudaGetLastError() == cudaSuccess ? ACCSPMM_SUCCESS : ACCSPMM_ERROR_CUDA;
         }
         // the B rows of the tile group two ahead are prefetched into L2
-        // (ACCSPMM_PREFETCH=0 turns it off): 2.02 against 2.06 ms per step at
-        // K = 128, 3.87 against 4.01 ms at K = 256, bit-identical
+        // (ACCSPMM_PREFETCH=0 turns it off): 1.99 against 2.06 ms per step at
+        // K = 128, 3.82 against 4.01 ms at K = 256, bit-identical
         if (st == ACCSPMM_SUCCESS)
             st = env_int("ACCSPMM_PREFETCH", 1) ? launch_packed_t<128, DirectBatch<128>::U, 2, true>(a, s)
                                                 : launch_packed_t<128, DirectBatch<128>::U, 2>(a, s);

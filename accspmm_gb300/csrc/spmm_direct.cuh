@@ -202,7 +202,8 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
             for (int j = 0; j < MA; ++j) {
                 uint32_t e = 32 * j + lane;
                 uint32_t tile = t + e / 8;
-                ma[j] = (e < 8 * U && tile < te) ? __ldg(a.a2b + size_t(t) * 8 + e) : kPad;
+                // PF: lanes 8U .. 16U - 1 take the entries of the group after
+                ma[j] = (e < (PF ? 16 * U : 8 * U) && tile < te) ? __ldg(a.a2b + size_t(t) * 8 + e) : kPad;
             }
             uint32_t tl = t + uint32_t(lane);
             bool ok = lane < U && tl < te;
@@ -249,25 +250,18 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
             n0[u] = (v0 && fok[0]) ? ldg_u2_ordered(w0 + nb_off) : zero;
             n1[u] = (v1 && fok[0]) ? ldg_u2_ordered(w1 + nb_off) : zero;
         };
-        // PF: sparseA2B entry `lane` of the group two ahead of the issue group
-        static_assert(!PF || 8 * U <= 32, "one prefetched row per lane");
-        uint32_t mp = kPad;
-        auto load_pf = [&](uint32_t t) {
-            if (PF) {
-                const uint32_t tile = t + uint32_t(lane) / 8;
-                mp = (lane < 8 * U && tile < te) ? __ldg(a.a2b + size_t(t) * 8 + lane) : kPad;
-            }
-        };
+        // PF: lane 8U + e holds sparseA2B entry e of the group after the one
+        // that load_meta fetched for issue, two groups ahead of the loads
+        static_assert(!PF || (MA == 1 && 16 * U <= 32), "one prefetched row per lane");
         auto prefetch_rows = [&]() {
-            if (PF && mp < a.cols) {
-                const uint8_t* r = a.bp + size_t(mp) * a.bpitch + 320 * (blk.f0 / 128);
+            if (PF && lane >= 8 * U && ma[0] < a.cols) {
+                const uint8_t* r = a.bp + size_t(ma[0]) * a.bpitch + 320 * (blk.f0 / 128);
                 asm volatile("cp.async.bulk.prefetch.L2.global [%0], 320;" ::"l"(r) : "memory");
             }
         };
 #pragma unroll
         for (int u = 0; u < U; ++u) issue(u);
         load_meta(tb + U);  // padding when past te
-        load_pf(tb + 2 * U);
         for (uint32_t t = tb; t < te; t += U) {
 #pragma unroll
             for (int u = 0; u < U; ++u) {
@@ -287,7 +281,6 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
                 if (u == 0) prefetch_rows();  // tiles t + 2U .. t + 3U - 1
             }
             load_meta(t + 2 * U);
-            load_pf(t + 3 * U);
         }
         blk.template flush<false>(a, acc, wl, tb, te, first_win);
     }
