@@ -360,11 +360,12 @@ class DeviceMETCF(DeviceObject):
 
     def gather_floor(self, B, K: int, repeats: int = 10, stream=None, slice_width: int = 0) -> float:
         """Milliseconds of a launch that only gathers the B rows this SpMM
-        reads (accspmm_gather_floor), in the SpMM's launch shape or in the
+        reads (accspmm_gather_floor of the measurement build,
+        libaccspmm_lab.so), in the SpMM's launch shape or in the
         register-direct shape of another slice width."""
         ms = C.c_float(0.0)
-        call("accspmm_gather_floor", self.ref, C.c_void_p(_addr(B)), K, slice_width, repeats,
-             C.byref(ms), _stream(stream))
+        capi.call_lab("accspmm_gather_floor", self.ref, C.c_void_p(_addr(B)), K, slice_width, repeats,
+                      C.byref(ms), _stream(stream))
         return float(ms.value)
 
     def gcn_layer(self, H, k_in: int, W, k_out: int, out, bias=None,

@@ -13,6 +13,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 # ACCSPMM_LIB selects another build of the library (same ABI)
 LIB_PATH = os.environ.get("ACCSPMM_LIB") or os.path.join(PKG, "libaccspmm.so")
+# the measurement build: the same ABI plus the variant kernels and the gather floor
+LAB_PATH = os.path.join(PKG, "libaccspmm_lab.so")
 HEADER = os.path.join(ROOT, "include", "accspmm.h")
 
 u32 = C.c_uint32
@@ -39,6 +41,17 @@ ERROR_CANCELLED = 37
 ERROR_FORMAT = 38
 PREC_TF32 = 0
 PREC_3XTF32 = 1
+OPT_PACK = 0
+OPT_PREFETCH = 1
+OPT_SCHEDULE = 2
+OPT_SLICE_WIDTH = 3
+OPT_CTAS_PER_SM = 4
+OPT_TILE_RING = 5
+OPT_WINDOWS_PER_CTA = 6
+OPT_HOST_SLICE_WIDTH = 7
+OPT_HOST_DIRECT_C = 8
+OPT_KERNEL = 9
+KERNELS = {"direct": 0, "pipe": 1, "bulk": 2, "lean": 3, "db": 4, "tma": 5, "staged": 6}
 ACT_NONE = 0
 ACT_RELU = 1
 HOST = 0
@@ -144,9 +157,12 @@ _SIGS = {
     "accspmm_noalloc_max_c_rows": ([], C.c_uint32),
     "accspmm_time_spmm": ([C.POINTER(METCF), C.POINTER(ADPBME), vp, vp, u32, u32, i32, i32, i32,
                            f32p, vp], C.c_int),
+    "accspmm_set_option": ([i32, i32], C.c_int),
+    "accspmm_get_option": ([i32, C.POINTER(i32)], C.c_int),
 }
 
 _LIB = None
+_LAB = None
 
 
 class AccSpmmError(RuntimeError):
@@ -163,27 +179,76 @@ def header_functions() -> list:
     return sorted(set(re.findall(r"\b(accspmm_\w+)\s*\(", text)))
 
 
-def load():
-    """Loads libaccspmm.so; raises if it has not been built."""
-    global _LIB
-    if _LIB is not None:
-        return _LIB
-    if not os.path.exists(LIB_PATH):
-        raise RuntimeError(f"{LIB_PATH} is missing: build it with "
+def _open(path: str):
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with "
                            "`python -c 'import __graft_entry__ as g; g.build()'`")
-    lib = C.CDLL(LIB_PATH)
+    lib = C.CDLL(path)
     for name, (args, res) in _SIGS.items():
         fn = getattr(lib, name)
         fn.argtypes = args
         fn.restype = res
-    _LIB = lib
     return lib
 
 
-def check(fn: str, status: int) -> None:
+def load():
+    """Loads libaccspmm.so; raises if it has not been built."""
+    global _LIB
+    if _LIB is None:
+        _LIB = _open(LIB_PATH)
+    return _LIB
+
+
+def load_lab():
+    """Loads the measurement build libaccspmm_lab.so (the same ABI with the
+    variant kernels selectable through OPT_KERNEL, and accspmm_gather_floor);
+    raises if it has not been built."""
+    global _LAB
+    if _LAB is None:
+        _LAB = _open(LAB_PATH)
+    return _LAB
+
+
+def check(fn: str, status: int, lib=None) -> None:
     if status != SUCCESS:
-        raise AccSpmmError(fn, status, load().accspmm_last_error().decode())
+        raise AccSpmmError(fn, status, (lib or load()).accspmm_last_error().decode())
 
 
 def call(name: str, *args) -> None:
     check(name, getattr(load(), name)(*args))
+
+
+def call_lab(name: str, *args) -> None:
+    lab = load_lab()
+    check(name, getattr(lab, name)(*args), lab)
+
+
+def get_option(option: int, lib=None) -> int:
+    v = C.c_int32()
+    lib = lib or load()
+    check("accspmm_get_option", lib.accspmm_get_option(option, C.byref(v)), lib)
+    return v.value
+
+
+def set_option(option: int, value: int, lib=None) -> None:
+    lib = lib or load()
+    check("accspmm_set_option", lib.accspmm_set_option(option, value), lib)
+
+
+class option:
+    """Context manager: an option set for the duration of a block, restored after.
+
+        with capi.option(capi.OPT_PACK, 0):
+            m.spmm(B, C, K)
+    """
+
+    def __init__(self, opt: int, value: int, lib=None):
+        self.opt, self.value, self.lib = opt, value, lib
+
+    def __enter__(self):
+        self.old = get_option(self.opt, self.lib)
+        set_option(self.opt, self.value, self.lib)
+        return self
+
+    def __exit__(self, *exc):
+        set_option(self.opt, self.old, self.lib)

@@ -8,6 +8,7 @@
 #include "accspmm.h"
 #include "common.hpp"
 #include "host_formats.hpp"
+#include "options.hpp"
 #include "spmm_internal.hpp"
 
 using namespace accspmm;
@@ -383,7 +384,27 @@ int accspmm_spmm_chain(const accspmm_metcf_t* metcf, const float* B, float* C, u
 int accspmm_gather_floor(const accspmm_metcf_t* metcf, const float* B, uint32_t K,
                          uint32_t slice_width, int32_t repeats, float* avg_ms, void* stream) {
     clear_error();
+#ifdef ACCSPMM_LAB
     return gather_floor_impl(metcf, B, K, slice_width, repeats, avg_ms, stream);
+#else
+    (void)metcf, (void)B, (void)K, (void)slice_width, (void)repeats, (void)avg_ms, (void)stream;
+    ACC_FAIL(ACCSPMM_ERROR_UNSUPPORTED,
+             "accspmm_gather_floor is a measurement entry point of libaccspmm_lab.so");
+#endif
+}
+
+int accspmm_set_option(int32_t option, int32_t value) {
+    clear_error();
+    return set_option(option, value);
+}
+
+int accspmm_get_option(int32_t option_id, int32_t* value) {
+    clear_error();
+    if (!value) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "null argument");
+    if (option_id < 0 || option_id > ACCSPMM_OPT_KERNEL)
+        ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "unknown option %d", option_id);
+    *value = option(option_id);
+    return ACCSPMM_SUCCESS;
 }
 
 int accspmm_spmm_host(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp,

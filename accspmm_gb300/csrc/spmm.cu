@@ -31,8 +31,10 @@
 
 #include "common.hpp"
 #include "device_util.cuh"
+#include "mbarrier.cuh"
 #include "spmm_common.cuh"
 #include "spmm_direct.cuh"
+#include "options.hpp"
 #include "spmm_internal.hpp"
 
 namespace accspmm {
@@ -41,8 +43,6 @@ namespace {
 
 constexpr int kNW = kDirectNW;  // warps per CTA of the register-direct kernels
 
-// Zero source for the padding rows of a tile (FS <= 128 floats).
-__device__ __align__(16) float g_zero_row_direct[128] = {0.f};
 
 
 // One-matrix launch of the register-direct kernel: one CTA per work item.
@@ -82,8 +82,12 @@ __global__ void __launch_bounds__(NW * 32, MINB) spmm_window_packed_kernel(const
 // holding value j's bits in its high nibble for even j, low nibble for odd.
 // One float4 of B per thread and step, read once with a streaming load.
 __global__ void pack_tf32_kernel(const float4* __restrict__ B, uint8_t* __restrict__ P, uint32_t K,
-                                 uint32_t pitch, size_t n4) {
+                                 uint32_t pitch, size_t n4, uint8_t* __restrict__ zero_row) {
     const uint32_t k4 = K / 4;
+    // the zero row read for padding columns (pitch is a multiple of 8)
+    if (blockIdx.x == 0)
+        for (uint32_t j = threadIdx.x; j < pitch / 8; j += blockDim.x)
+            reinterpret_cast<uint2*>(zero_row)[j] = make_uint2(0u, 0u);
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n4;
          i += size_t(gridDim.x) * blockDim.x) {
         const size_t row = i / k4;
@@ -100,6 +104,10 @@ __global__ void pack_tf32_kernel(const float4* __restrict__ B, uint8_t* __restri
                      (((r3 >> 12) & 0x0Fu) << 8));
     }
 }
+
+#ifdef ACCSPMM_LAB
+// Zero source for the padding rows of a tile (FS <= 128 floats).
+__device__ __align__(16) float g_zero_row_direct[128] = {0.f};
 
 // Double-buffered register-direct kernel: the gathers of batch q + 1 are
 // issued before the MMAs of batch q, so every warp keeps a batch of B rows
@@ -238,25 +246,71 @@ int launch_db(const SpmmArgs& a, cudaStream_t s) {
     return ACCSPMM_SUCCESS;
 }
 
-// rwo[w] = first tile whose window start row (row_indices, non-decreasing)
-// is >= 8w, for w in [0, Weff]: one thread per window, binary search over the
-// tiles.  Tiles that claim windows >= Weff, or a decreasing row_indices, raise
-// *err.
+#endif  // ACCSPMM_LAB
+
+// Sticky status of the SpMM calls on this device, reported and cleared by
+// accspmm_device_status: kStatusTimeout -- a bounded wait on an asynchronous
+// copy expired; kStatusRowsPastC -- an adaptive call's rowIndices named windows
+// at or past c_rows / 8, whose tiles were left out of C; kStatusUnsorted -- an
+// adaptive call's rowIndices were not non-decreasing multiples of 8 (tiles may
+// have been summed into the wrong windows).
+constexpr unsigned kStatusTimeout = 1u, kStatusRowsPastC = 2u, kStatusUnsorted = 4u;
+__device__ unsigned int g_spmm_status = 0;
+
+// The adaptive path's window offsets from an AdpBME's rowIndices, plus the
+// checks of rowIndices that the derivation relies on, in one pass of
+// max(T, Weff + 1) threads:
+//  - thread w <= Weff: rwo[w] = first tile whose window start row is >= 8w (a
+//    binary search; for any rowIndices the result is monotone in w and within
+//    [0, T], so the SpMM reads only valid tiles whatever the input), and
+//    w == Weff raises kStatusRowsPastC if tiles remain past the last window;
+//  - thread t < T: rowIndices[t] must be a multiple of 8 not below
+//    rowIndices[t - 1] (CSR2AdpBME writes the first row of each tile's window,
+//    window by window, include/format.hpp:364), else kStatusUnsorted.
+// Raised bits go to *err (when non-null) and, when `sticky`, to the device
+// status word as well.
 __global__ void rwo_from_row_indices_kernel(const uint32_t* __restrict__ ri, uint32_t T,
                                             uint32_t Weff, uint32_t* __restrict__ rwo,
-                                            uint32_t* __restrict__ err) {
-    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w > Weff) return;
-    const uint64_t row = uint64_t(w) * kWin;
-    uint32_t lo = 0, hi = T;
-    while (lo < hi) {
-        const uint32_t mid = lo + (hi - lo) / 2;
-        if (uint64_t(ri[mid]) < row) lo = mid + 1;
-        else hi = mid;
+                                            uint32_t* __restrict__ err, int sticky) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned bits = 0;
+    if (i <= Weff) {
+        const uint64_t row = uint64_t(i) * kWin;
+        uint32_t lo = 0, hi = T;
+        while (lo < hi) {
+            const uint32_t mid = lo + (hi - lo) / 2;
+            if (uint64_t(ri[mid]) < row) lo = mid + 1;
+            else hi = mid;
+        }
+        rwo[i] = lo;
+        if (i == Weff && lo < T) bits |= kStatusRowsPastC;
     }
-    rwo[w] = lo;
-    if (w == Weff && lo < T) atomicOr(err, 1u);
-    if (w < Weff && lo < T && lo > 0 && ri[lo] < ri[lo - 1]) atomicOr(err, 2u);
+    if (i < T) {
+        const uint32_t r = ri[i];
+        if ((r % kWin) != 0 || (i > 0 && ri[i - 1] > r)) bits |= kStatusUnsorted;
+    }
+    // one atomic per warp at most
+    const unsigned any = __reduce_or_sync(0xffffffffu, bits);
+    if (any && (threadIdx.x & 31) == 0) {
+        if (err) atomicOr(err, any);
+        if (sticky) atomicOr(&g_spmm_status, any);
+    }
+}
+
+// The failure path of the bounded waits, exercised on purpose: one warp
+// waits on an mbarrier that nothing arrives on.  The wait gives up after
+// limit_ns, the kernel records kStatusTimeout and returns; nothing traps and
+// the context stays usable.
+__global__ void bounded_wait_selftest_kernel(uint64_t limit_ns) {
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t b = smem_addr(&bar);
+    if (threadIdx.x == 0) {
+        mbar_init(b, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const bool landed = mbar_wait(b, 0u, limit_ns);  // phase 0 never completes
+    if (!__all_sync(0xffffffffu, landed) && threadIdx.x == 0) atomicOr(&g_spmm_status, kStatusTimeout);
 }
 
 // Heaviest-first schedule of nb window blocks of wb windows: order[i] = the
@@ -370,15 +424,57 @@ void schedule_cache_forget(const uint32_t* rwo) {
 }
 
 int rwo_from_row_indices(const uint32_t* ri, uint32_t T, uint32_t W, uint32_t* rwo, uint32_t* err,
-                         cudaStream_t s) {
-    rwo_from_row_indices_kernel<<<(W + 1 + 255) / 256, 256, 0, s>>>(ri, T, W, rwo, err);
+                         bool sticky, cudaStream_t s) {
+    const uint64_t n = std::max<uint64_t>(uint64_t(W) + 1, T);
+    rwo_from_row_indices_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(ri, T, W, rwo, err, sticky ? 1 : 0);
     ACC_LAUNCH_CHECK();
+    return ACCSPMM_SUCCESS;
+}
+
+int bounded_wait_selftest(uint32_t limit_ms, cudaStream_t s) {
+    if (limit_ms == 0 || limit_ms > 2000)
+        ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "limit_ms must be in [1, 2000]");
+    bounded_wait_selftest_kernel<<<1, 32, 0, s>>>(uint64_t(limit_ms) * 1000000ull);
+    ACC_LAUNCH_CHECK();
+    return ACCSPMM_SUCCESS;
+}
+
+int device_status_impl(void* stream) {
+    ACC_CUDA(cudaStreamSynchronize(as_stream(stream)));
+    unsigned int v = 0;
+    ACC_CUDA(cudaMemcpyFromSymbol(&v, g_spmm_status, sizeof v));
+    if (v) {
+        const unsigned int z = 0;
+        ACC_CUDA(cudaMemcpyToSymbol(g_spmm_status, &z, sizeof z));
+    }
+#ifdef ACCSPMM_LAB
+    unsigned int vb = 0;
+    if (int st = bulk_status_take(&vb)) return st;
+    if (vb) v |= kStatusTimeout;
+#endif
+    if (v & (kStatusRowsPastC | kStatusUnsorted))
+        ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "an adaptive SpMM call since the last check had inconsistent rowIndices:%s%s%s",
+                 (v & kStatusRowsPastC) ? " tiles of windows at or past c_rows / 8 were left out of C (c_rows too small);" : "",
+                 (v & kStatusUnsorted) ? " rowIndices are not non-decreasing multiples of 8;" : "",
+                 (v & kStatusTimeout) ? " a bounded wait also expired" : "");
+    if (v & kStatusTimeout) ACC_FAIL(ACCSPMM_ERROR_TIMEOUT, "a bounded wait in the SpMM kernels expired");
     return ACCSPMM_SUCCESS;
 }
 
 namespace {
 
-enum KernelKind { kDirect = 0, kPipe = 1, kBulk = 2, kLean = 3, kDb = 4, kTma = 5 };
+// Kernel kinds, the values of ACCSPMM_OPT_KERNEL.  The product library
+// builds only kDirect (the register-direct kernels, with or without packed
+// B); the others are measurement variants built into libaccspmm_lab.so.
+enum KernelKind {
+    kDirect = ACCSPMM_KERNEL_DIRECT,
+    kPipe = ACCSPMM_KERNEL_PIPE,
+    kBulk = ACCSPMM_KERNEL_BULK,
+    kLean = ACCSPMM_KERNEL_LEAN,
+    kDb = ACCSPMM_KERNEL_DB,
+    kTma = ACCSPMM_KERNEL_TMA,
+    kStaged = ACCSPMM_KERNEL_STAGED
+};
 
 struct Config {
     int kernel;
@@ -391,13 +487,6 @@ struct Config {
     uint32_t slice_major;
     int pack;  // TF32 ring at 128-column slices: gather from a packed copy of B (-1 by the default rule, 0 off, 1 on)
 };
-
-int env_int(const char* name, int dflt) {
-    const char* e = std::getenv(name);
-    return e && *e ? std::atoi(e) : dflt;
-}
-
-int env_int(const char* name, int dflt);
 
 // Tuned launch shapes, by matrix signature (autotune below).
 struct TuneKey {
@@ -422,8 +511,8 @@ thread_local const Config* g_forced = nullptr;
 //    (the ring spills there);
 //  - K <= 32: 32-column slices at 3 CTAs per SM, batch then compute.
 // A shape found by accspmm_autotune_metcf for the same signature replaces
-// the default; environment variables override both for experiments
-// (ACCSPMM_KERNEL, _FS, _OCC, _ROLL, _WB, _NW, _ORDER, _HINTS).
+// the default; the launch options (accspmm_set_option: slice width, CTAs
+// per SM, tile ring, windows per CTA, packing) override both.
 Config choose_config(uint32_t W, uint32_t T, uint32_t K, int precision) {
     if (g_forced) return *g_forced;
     Config c;
@@ -446,28 +535,21 @@ Config choose_config(uint32_t W, uint32_t T, uint32_t K, int precision) {
         auto it = g_tuned.find(TuneKey{W, T, K, precision});
         if (it != g_tuned.end()) c = it->second;
     }
-    if (const char* e = std::getenv("ACCSPMM_KERNEL"))
-        c.kernel = std::strcmp(e, "pipe") == 0   ? kPipe
-                   : std::strcmp(e, "bulk") == 0 ? kBulk
-                   : std::strcmp(e, "lean") == 0 ? kLean
-                   : std::strcmp(e, "db") == 0   ? kDb
-                   : std::strcmp(e, "tma") == 0  ? kTma
-                                                 : kDirect;
-    int fs = env_int("ACCSPMM_FS", 0);
-    if (fs == 32 || fs == 64 || fs == 128) c.fs = fs;
-    int occ = env_int("ACCSPMM_OCC", 0);
-    if (occ == 2 || occ == 3) c.occ = occ;
-    int nw = env_int("ACCSPMM_NW", 0);
+    c.kernel = option(ACCSPMM_OPT_KERNEL) != kDirect ? option(ACCSPMM_OPT_KERNEL) : c.kernel;
+    if (const int fs = option(ACCSPMM_OPT_SLICE_WIDTH)) c.fs = fs;
+    if (const int occ = option(ACCSPMM_OPT_CTAS_PER_SM)) c.occ = occ;
+    if (const int ring = option(ACCSPMM_OPT_TILE_RING); ring >= 0) c.ring = ring;
+    if (const int wb = option(ACCSPMM_OPT_WINDOWS_PER_CTA)) c.wb = uint32_t(wb);
+    if (const int pk = option(ACCSPMM_OPT_PACK); pk >= 0) c.pack = pk;
+#ifdef ACCSPMM_LAB
+    // shape details of the measurement variants
+    const int nw = lab_env("ACCSPMM_NW", 0);
     if (nw == 2 || nw == 4 || nw == 8) c.nw = nw;
     if (c.kernel == kPipe && c.fs >= 64) c.nw = 4;  // stage ring must fit in shared memory
     if ((c.kernel == kBulk || c.kernel == kTma) && c.nw == 8) c.nw = 4;
-    c.hints = env_int("ACCSPMM_HINTS", c.hints) ? 1 : 0;
-    int wbe = env_int("ACCSPMM_WB", 0);
-    if (wbe >= 1 && wbe <= 1024) c.wb = uint32_t(wbe);
-    const int pk = env_int("ACCSPMM_PACK", -1);  // 0 never pack B, 2 pack wherever the launch shape allows
-    if (pk == 0) c.pack = 0;
-    if (pk == 2) c.pack = 1;
-    if (const char* e = std::getenv("ACCSPMM_ORDER")) c.slice_major = std::strcmp(e, "slice") == 0;
+    c.hints = lab_env("ACCSPMM_HINTS", c.hints) ? 1 : 0;
+    c.slice_major = lab_env("ACCSPMM_ORDER_SLICE", 0) ? 1u : 0u;
+#endif
     return c;
 }
 
@@ -505,8 +587,7 @@ int launch_direct(const SpmmArgs& a, int occ, int ring, cudaStream_t s) {
     const bool epi = a.bias != nullptr || a.act != 0;
     if (occ == 3) {
         constexpr int U = (DirectBatch<FS>::U + 1) / 2;
-        const int roll = env_int("ACCSPMM_ROLL", ring);
-        const bool use_roll = roll < 0 ? kRollDefault<FS, PREC, 3> : roll != 0;
+        const bool use_roll = ring < 0 ? kRollDefault<FS, PREC, 3> : ring != 0;
         if (use_roll) {
             if (epi) return launch_direct_t<FS, PREC, U, 3, true, kNW, true>(a, s);
             return launch_direct_t<FS, PREC, U, 3, false, kNW, true>(a, s);
@@ -515,8 +596,7 @@ int launch_direct(const SpmmArgs& a, int occ, int ring, cudaStream_t s) {
         return launch_direct_t<FS, PREC, U, 3, false>(a, s);
     }
     constexpr int U = DirectBatch<FS>::U;
-    const int roll = env_int("ACCSPMM_ROLL", ring);
-    if (roll < 0 ? kRollDefault<FS, PREC, 2> : roll != 0) {
+    if (ring < 0 ? kRollDefault<FS, PREC, 2> : ring != 0) {
         if (epi) return launch_direct_t<FS, PREC, U, 2, true, kNW, true>(a, s);
         return launch_direct_t<FS, PREC, U, 2, false, kNW, true>(a, s);
     }
@@ -622,20 +702,21 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     // SpMM took 53.0 us instead of 62.0 us.
     if (stable_rwo && !cfg.slice_major && a.n_wblocks <= kOrderMaxBlocks &&
         uint64_t(a.n_wblocks) * a.n_slices <= uint64_t(kOrderMaxWaves) * sm_count() * uint32_t(cfg.occ) &&
-        env_int("ACCSPMM_SCHEDULE", 1) != 0) {
+        option(ACCSPMM_OPT_SCHEDULE) != 0) {
         int st = cached_order(rwo, W, cfg.wb, a.n_wblocks, s, &a.order);
         if (st) return st;
     }
     // only the register-direct kernel has the epilogue; it cuts the matrix
     // into the same pieces as the other variants
     if (epi.bias || epi.act) cfg.kernel = kDirect;
+    const bool x3 = precision == ACCSPMM_PREC_3XTF32;
+#ifdef ACCSPMM_LAB
     if (cfg.kernel == kPipe) return launch_pipe(a, cfg.fs, precision, cfg.nw, cfg.hints, s);
     if (cfg.kernel == kBulk) return launch_bulk(a, cfg.fs, precision, cfg.nw, cfg.hints, s);
     if (cfg.kernel == kTma) return launch_tma(a, cfg.fs, precision, cfg.nw, s);
-    if (cfg.kernel == kLean) return launch_lean(a, cfg.fs, precision, env_int("ACCSPMM_MINB", 4), s);
+    if (cfg.kernel == kLean) return launch_lean(a, cfg.fs, precision, lab_env("ACCSPMM_MINB", 4), s);
     if (cfg.kernel == kDb) {
-        const bool x3 = precision == ACCSPMM_PREC_3XTF32;
-        const int u = env_int("ACCSPMM_U", 0);
+        const int u = lab_env("ACCSPMM_U", 0);
         switch (cfg.fs) {
             case 32: return x3 ? launch_db<32, ACCSPMM_PREC_3XTF32, 4>(a, s) : launch_db<32, ACCSPMM_PREC_TF32, 4>(a, s);
             case 64:
@@ -644,7 +725,22 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
             default: return x3 ? launch_db<128, ACCSPMM_PREC_3XTF32, 1>(a, s) : launch_db<128, ACCSPMM_PREC_TF32, 1>(a, s);
         }
     }
-    const bool x3 = precision == ACCSPMM_PREC_3XTF32;
+    if (cfg.kernel == kStaged) {
+        // the slice-major staged kernel covers whole launches in TF32 only
+        const bool whole = slice_begin == 0 && uint64_t(slice_count) * uint32_t(cfg.fs) >= K;
+        if (!x3 && whole) {
+            cudaMemPool_t pool;
+            int st = library_pool(&pool);
+            if (st) return st;
+            void* S = nullptr;
+            ACC_CUDA(cudaMallocFromPoolAsync(&S, staged_bytes(cols, K), pool, s));
+            st = spmm_staged_launch(a, B, static_cast<float*>(S), uint32_t(lab_env("ACCSPMM_STAGE_V", 0)), s);
+            cudaFreeAsync(S, s);
+            if (st) ACC_FAIL(st, "staged SpMM launch failed");
+            return ACCSPMM_SUCCESS;
+        }
+    }
+#endif
     const int occ = cfg.occ;
     // TF32 at 128-column slices with the ring: B is first rounded to TF32 and
     // packed to 2.5 bytes a value (pack_tf32_kernel), so the SpMM gathers 10
@@ -656,8 +752,7 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     // 64-column slices (K = 64) a 3-byte packing cost what the gathers saved,
     // and a B that fits the L2 (the 16,384-row matrix, 53.5 against 52.0 us)
     // only gains a pass.  The autotuner times both ways.
-    const int roll = env_int("ACCSPMM_ROLL", cfg.ring);
-    const bool ring_on = roll < 0 || roll != 0;
+    const bool ring_on = cfg.ring != 0;
     const uint64_t b_bytes = uint64_t(cols) * K * 4;
     const bool pack_rule = cfg.pack > 0 || (cfg.pack < 0 && b_bytes >= (uint64_t(128) << 20));
     if (allow_pack && !x3 && !(epi.bias || epi.act) && ring_on && cfg.fs == 128 && occ == 2 && pack_rule) {
@@ -666,22 +761,21 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
         if (st) return st;
         const uint32_t pitch = 320 * ((K + 127) / 128);
         void* packed = nullptr;
-        ACC_CUDA(cudaMallocFromPoolAsync(&packed, size_t(cols) * pitch + 64, pool, s));
+        ACC_CUDA(cudaMallocFromPoolAsync(&packed, (size_t(cols) + 1) * pitch + 64, pool, s));
         a.bp = static_cast<const uint8_t*>(packed);
         a.bpitch = pitch;
         const size_t n4 = size_t(cols) * (K / 4);
-        const unsigned blocks = unsigned(std::min<size_t>((n4 + 255) / 256, size_t(sm_count()) * 16));
-        if (n4) {
-            pack_tf32_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(B),
-                                                    static_cast<uint8_t*>(packed), K, pitch, n4);
-            st = cudaGetLastError() == cudaSuccess ? ACCSPMM_SUCCESS : ACCSPMM_ERROR_CUDA;
-        }
+        const unsigned blocks = unsigned(std::min<size_t>((n4 + 255) / 256 + 1, size_t(sm_count()) * 16));
+        // the packed rows, then the zero row at index cols that padding reads
+        pack_tf32_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(B), static_cast<uint8_t*>(packed),
+                                                K, pitch, n4, static_cast<uint8_t*>(packed) + size_t(cols) * pitch);
+        st = cudaGetLastError() == cudaSuccess ? ACCSPMM_SUCCESS : ACCSPMM_ERROR_CUDA;
         // the B rows of the tile group two ahead are prefetched into L2
-        // (ACCSPMM_PREFETCH=0 turns it off): 1.99 against 2.06 ms per step at
-        // K = 128, 3.82 against 4.01 ms at K = 256, bit-identical
+        // (ACCSPMM_OPT_PREFETCH = 0 turns it off): 1.99 against 2.06 ms per
+        // step at K = 128, 3.82 against 4.01 ms at K = 256, bit-identical
         if (st == ACCSPMM_SUCCESS)
-            st = env_int("ACCSPMM_PREFETCH", 1) ? launch_packed_t<128, DirectBatch<128>::U, 2, true>(a, s)
-                                                : launch_packed_t<128, DirectBatch<128>::U, 2>(a, s);
+            st = option(ACCSPMM_OPT_PREFETCH) ? launch_packed_t<128, DirectBatch<128>::U, 2, true>(a, s)
+                                              : launch_packed_t<128, DirectBatch<128>::U, 2>(a, s);
         cudaFreeAsync(packed, s);
         if (st) ACC_FAIL(st, "packed SpMM launch failed");
         return ACCSPMM_SUCCESS;
@@ -748,6 +842,7 @@ struct RwoKey {
 };
 struct RwoEntry {
     uint32_t* rwo = nullptr;  // [weff + 2]: offsets, then an error word
+    uint32_t err = 0;         // that error word, read once when the offsets were derived
 };
 std::mutex g_rwo_mu;
 std::map<RwoKey, RwoEntry> g_rwo_cache;
@@ -771,11 +866,13 @@ int cached_rwo(const accspmm_adpbme_t* ad, uint32_t Weff, cudaStream_t s, const 
         ACC_CUDA(cudaMalloc(&e.rwo, (size_t(Weff) + 2) * 4));
         cudaError_t ce = cudaMemsetAsync(e.rwo + Weff + 1, 0, 4, s);
         if (ce == cudaSuccess) {
-            rwo_from_row_indices_kernel<<<(Weff + 1 + 255) / 256, 256, 0, s>>>(
-                ad->row_indices, ad->num_tiles, Weff, e.rwo, e.rwo + Weff + 1);
+            const uint64_t n = std::max<uint64_t>(uint64_t(Weff) + 1, ad->num_tiles);
+            rwo_from_row_indices_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(
+                ad->row_indices, ad->num_tiles, Weff, e.rwo, e.rwo + Weff + 1, 0);
             ce = cudaGetLastError();
         }
         if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+        if (ce == cudaSuccess) ce = cudaMemcpy(&e.err, e.rwo + Weff + 1, 4, cudaMemcpyDeviceToHost);
         if (ce != cudaSuccess) {
             cudaStreamSynchronize(s);
             cudaFree(e.rwo);
@@ -783,6 +880,14 @@ int cached_rwo(const accspmm_adpbme_t* ad, uint32_t Weff, cudaStream_t s, const 
         }
         it = g_rwo_cache.emplace(key, e).first;
     }
+    // a library-built AdpBME always passes; the check matters for one loaded
+    // from a file or copied from a caller's arrays
+    if (it->second.err & kStatusUnsorted)
+        ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "AdpBME rowIndices are not non-decreasing multiples of 8");
+    if (it->second.err & kStatusRowsPastC)
+        ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE,
+                 "c_rows=%u leaves tiles of later windows out of C: it must be at least the last rowIndices "
+                 "entry + 8 (accspmm_adaptive_c_rows)", Weff * kWin);
     *out = it->second.rwo;
     return ACCSPMM_SUCCESS;
 }
@@ -824,14 +929,14 @@ int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uin
                                   (ad->rows + kWin - 1) / kWin, T, ad->cols, B, C, K, precision, s, true,
                                   true);
     }
-    // a caller-filled object may change between calls: derive every time
-    DevBuf<uint32_t> scratch;  // rwo[Weff + 1] then an error word
-    ACC_CUDA(scratch.alloc(size_t(Weff) + 2, s));
+    // a caller-filled object may change between calls: derive every time,
+    // in stream order (inconsistent rowIndices raise the device status word
+    // that accspmm_device_status reports; no host wait here)
+    DevBuf<uint32_t> scratch;  // rwo[Weff + 1]
+    ACC_CUDA(scratch.alloc(size_t(Weff) + 1, s));
     uint32_t* rwo = scratch.p;
-    uint32_t* err = scratch.p + Weff + 1;
-    ACC_CUDA(cudaMemsetAsync(err, 0, 4, s));
-    rwo_from_row_indices_kernel<<<(Weff + 1 + 255) / 256, 256, 0, s>>>(ad->row_indices, T, Weff, rwo, err);
-    ACC_LAUNCH_CHECK();
+    st = rwo_from_row_indices(ad->row_indices, T, Weff, rwo, nullptr, true, s);
+    if (st) return st;
     return spmm_window_launch(rwo, ad->tc_offset, ad->tc_local_bit, ad->sparse_a2b, ad->data, Weff,
                               (ad->rows + kWin - 1) / kWin, T, ad->cols, B, C, K, precision, s, false,
                               true);
@@ -846,13 +951,18 @@ int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uin
 // rowWindowOffset derived from rowIndices plus a status word) lives in the
 // file-scope array below, which every GPU that loads the library holds until
 // the process exits.  All calls share the array, so calls that overlap on the
-// GPU (different streams, no ordering between them) race on it.
+// GPU (different streams, no ordering between them) race on it.  It never
+// packs B (that copy would need a scratch the size of B), so on a B of
+// 128 MiB or more at K > 64 it runs the kernel that reads fp32 B: the same
+// bits, 2.29 against 1.95 ms on the 1M-row power-law matrix at K = 128.
 // ---------------------------------------------------------------------------
 constexpr uint32_t kNoAllocWords = 1u << 20;  // 4 MiB: windows + 2 words
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocWords];
 
 // Device address of g_noalloc_scratch on the current device, looked up once
-// per device (the host-side symbol is not a device address).
+// per device (the host-side symbol is not a device address) and kept for the
+// life of the process: it belongs to the device's primary context, so it does
+// not survive a cudaDeviceReset of that device.
 static int noalloc_scratch(uint32_t** out) {
     static std::mutex mu;
     static uint32_t* ptr[64] = {nullptr};
@@ -890,11 +1000,11 @@ int spmm_adaptive_noalloc_impl(const accspmm_adpbme_t* ad, const float* B, float
     uint32_t* scratch = nullptr;
     st = noalloc_scratch(&scratch);
     if (st) return st;
-    uint32_t* rwo = scratch;             // [Weff + 1], fully rewritten below
-    uint32_t* err = scratch + Weff + 1;  // must start at zero
-    ACC_CUDA(cudaMemsetAsync(err, 0, 4, s));
-    rwo_from_row_indices_kernel<<<(Weff + 1 + 255) / 256, 256, 0, s>>>(ad->row_indices, T, Weff, rwo, err);
-    ACC_LAUNCH_CHECK();
+    uint32_t* rwo = scratch;  // [Weff + 1], fully rewritten below
+    // inconsistent rowIndices raise the device status word that
+    // accspmm_device_status reports (no host wait, nothing else to clear)
+    st = rwo_from_row_indices(ad->row_indices, T, Weff, rwo, nullptr, true, s);
+    if (st) return st;
     return spmm_window_launch(rwo, ad->tc_offset, ad->tc_local_bit, ad->sparse_a2b, ad->data, Weff,
                               (ad->rows + kWin - 1) / kWin, T, ad->cols, B, C, K, precision, s);
 }
@@ -916,7 +1026,11 @@ int autotune_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K
     std::vector<Config> cand;
     // (kernel, CTAs per SM, tile ring): register-direct at 3 and 2 CTAs per
     // SM with and without the rolling ring, double-buffered at 2
-    const int shapes[5][3] = {{kDirect, 3, 1}, {kDirect, 3, 0}, {kDirect, 2, 1}, {kDirect, 2, 0}, {kDb, 2, 0}};
+#ifdef ACCSPMM_LAB
+    const int shapes[][3] = {{kDirect, 3, 1}, {kDirect, 3, 0}, {kDirect, 2, 1}, {kDirect, 2, 0}, {kDb, 2, 0}};
+#else
+    const int shapes[][3] = {{kDirect, 3, 1}, {kDirect, 3, 0}, {kDirect, 2, 1}, {kDirect, 2, 0}};
+#endif
     for (const auto& ko : shapes)
         for (int fs : {32, 64, 128}) {
             if (fs > 32 && uint32_t(fs / 2) >= K) continue;  // slices far wider than K
@@ -995,7 +1109,6 @@ void autotune_clear() {
     g_tuned.clear();
 }
 
-int device_status_impl(void* stream) { return bulk_status(as_stream(stream), true); }
 
 int time_spmm_impl(const accspmm_metcf_t* m, const accspmm_adpbme_t* ad, const float* B, float* C,
                    uint32_t c_rows, uint32_t K, int precision, int warmup, int exe, float* avg_ms,

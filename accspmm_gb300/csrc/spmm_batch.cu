@@ -22,6 +22,7 @@
 #include "spmm_batch.hpp"
 #include "spmm_common.cuh"
 #include "spmm_direct.cuh"
+#include "options.hpp"
 #include "spmm_internal.hpp"
 
 namespace accspmm {
@@ -108,11 +109,11 @@ int launch_batch_t(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_item
 int batch_fs_for(uint32_t max_k) { return max_k <= 32 ? 32 : 64; }
 
 bool batch_item_is_wide(uint32_t K, int precision) {
-    static const bool off = [] {
-        const char* e = std::getenv("ACCSPMM_BATCH_WIDE");
-        return e && *e == '0';
-    }();
-    return !off && precision == ACCSPMM_PREC_TF32 && K > 64;
+#ifdef ACCSPMM_LAB
+    // measurement: ACCSPMM_BATCH_WIDE=0 runs wide items in the narrow group
+    if (lab_env("ACCSPMM_BATCH_WIDE", 1) == 0) return false;
+#endif
+    return precision == ACCSPMM_PREC_TF32 && K > 64;
 }
 
 int launch_batch(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items, uint32_t max_wb,
@@ -120,9 +121,13 @@ int launch_batch(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items,
     ACC_CUDA(cudaMemsetAsync(d_counter, 0, 4, s));
     const bool x3 = precision == ACCSPMM_PREC_3XTF32;
     // the rolling tile ring spills in the persistent kernel (24 bytes) and
-    // measured 6 % slower on 128 power-law graphs: off unless ACCSPMM_ROLL=1
-    const char* e = std::getenv("ACCSPMM_ROLL");
-    const bool roll = e && *e == '1';
+    // measured 6 % slower on 128 power-law graphs: off (the measurement build
+    // turns it on with ACCSPMM_BATCH_ROLL=1)
+#ifdef ACCSPMM_LAB
+    const bool roll = lab_env("ACCSPMM_BATCH_ROLL", 0) == 1;
+#else
+    const bool roll = false;
+#endif
     if (fs == 128) {
         // wide TF32 items: 128-column slices with the rolling tile ring, the
         // one-matrix default for K > 64

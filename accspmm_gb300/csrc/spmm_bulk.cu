@@ -28,20 +28,18 @@
 
 #include "common.hpp"
 #include "device_util.cuh"
+#include "mbarrier.cuh"
 #include "spmm_common.cuh"
 
 namespace accspmm {
 
 // Zero source for the padding rows of a tile (FS <= 128 floats).
 static __device__ __align__(16) float g_zero_row[128] = {0.f};
-// Sticky status of bounded waits that expired (0 = none).
+// Sticky status of this file's bounded waits that expired (0 = none), folded
+// into accspmm_device_status by bulk_status_take.
 static __device__ unsigned int g_bulk_status = 0;
 
 namespace {
-
-// A wait gives up after this long (the copies it waits for are a few KB of
-// valid global memory, normally landing within microseconds).
-constexpr uint64_t kWaitLimitNs = 2000000000ull;
 
 template <int FS>
 struct BulkCfg {
@@ -51,53 +49,6 @@ struct BulkCfg {
     static constexpr int kMeta = kU * 4;                            // (bits lo, hi, off, -) per tile
     static constexpr int kStage = kB + kMeta;                       // floats per stage
 };
-
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-    asm volatile(
-        "{\n\t.reg .b64 st;\n\t"
-        "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(bar),
-        "r"(bytes)
-        : "memory");
-}
-
-// One try_wait, suspending the thread for at most about 20 us.
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity), "r"(20000u)
-        : "memory");
-    return ok != 0;
-}
-
-__device__ __forceinline__ uint64_t global_ns() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Wait for a barrier phase, bounded by limit_ns of wall time; false if the
-// limit expired.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
-                                          uint64_t limit_ns = kWaitLimitNs) {
-    if (mbar_try_wait(bar, parity)) return true;
-    const uint64_t t0 = global_ns();
-    for (;;) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if (global_ns() - t0 > limit_ns) return false;
-    }
-}
 
 template <bool HINTS>
 __device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar,
@@ -588,43 +539,12 @@ int launch_bulk(const SpmmArgs& a, int fs, int precision, int nw, int hints, cud
                                             : launch_prec<ACCSPMM_PREC_TF32>(a, fs, nw, hints, s);
 }
 
-namespace {
-
-// The failure path of the bounded waits, exercised on purpose: one warp
-// waits on an mbarrier that nothing arrives on.  The wait gives up after
-// limit_ns, the kernel records ACCSPMM_ERROR_TIMEOUT in the status word and
-// returns; nothing traps and the context stays usable.
-__global__ void bounded_wait_selftest_kernel(uint64_t limit_ns) {
-    __shared__ __align__(8) uint64_t bar;
-    const uint32_t b = smem_addr(&bar);
-    if (threadIdx.x == 0) {
-        mbar_init(b, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    const bool landed = mbar_wait(b, 0u, limit_ns);  // phase 0 never completes
-    if (!__all_sync(0xffffffffu, landed) && threadIdx.x == 0) atomicOr(&g_bulk_status, 1u);
-}
-
-}  // namespace
-
-int bounded_wait_selftest(uint32_t limit_ms, cudaStream_t s) {
-    if (limit_ms == 0 || limit_ms > 2000)
-        ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "limit_ms must be in [1, 2000]");
-    bounded_wait_selftest_kernel<<<1, 32, 0, s>>>(uint64_t(limit_ms) * 1000000ull);
-    ACC_LAUNCH_CHECK();
-    return ACCSPMM_SUCCESS;
-}
-
-int bulk_status(cudaStream_t s, bool clear) {
-    ACC_CUDA(cudaStreamSynchronize(s));
-    unsigned int v = 0;
-    ACC_CUDA(cudaMemcpyFromSymbol(&v, g_bulk_status, sizeof v));
-    if (v && clear) {
-        unsigned int z = 0;
+int bulk_status_take(unsigned int* v) {
+    ACC_CUDA(cudaMemcpyFromSymbol(v, g_bulk_status, sizeof *v));
+    if (*v) {
+        const unsigned int z = 0;
         ACC_CUDA(cudaMemcpyToSymbol(g_bulk_status, &z, sizeof z));
     }
-    if (v) ACC_FAIL(ACCSPMM_ERROR_TIMEOUT, "a bounded wait in the SpMM kernel expired");
     return ACCSPMM_SUCCESS;
 }
 

@@ -432,10 +432,16 @@ int launch_pipe(const SpmmArgs& a, int fs, int precision, int nw, int hints, cud
 size_t pipe_smem_bytes(int fs, int nw, uint32_t wb);
 // Launch of the bulk-copy (TMA) kernel and its status word (spmm_bulk.cu).
 int launch_bulk(const SpmmArgs& a, int fs, int precision, int nw, int hints, cudaStream_t s);
-int bulk_status(cudaStream_t s, bool clear);
+// Reads and clears the bulk kernels' sticky wait status (after a stream sync).
+int bulk_status_take(unsigned int* v);
 // Launch of the tensor-map gather4 (TMA) kernel (spmm_bulk.cu).
 int launch_tma(const SpmmArgs& a, int fs, int precision, int nw, cudaStream_t s);
 // Launch of the occupancy-sized register-direct kernel (spmm_lean.cu).
 int launch_lean(const SpmmArgs& a, int fs, int precision, int minb, cudaStream_t s);
+// Slice-major SpMM over B staged in 32-column TF32 slices (spmm_slice.cu):
+// bytes of the staging buffer, and the staging pass + SpMM launch (all of
+// a's windows and K columns; S holds staged_bytes(a.cols, a.K) bytes).
+size_t staged_bytes(uint32_t cols, uint32_t K);
+int spmm_staged_launch(const SpmmArgs& a, const float* B, float* S, uint32_t variant, cudaStream_t s);
 
 }  // namespace accspmm

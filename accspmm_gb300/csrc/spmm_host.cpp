@@ -28,6 +28,7 @@
 
 #include "accspmm.h"
 #include "common.hpp"
+#include "options.hpp"
 #include "spmm_internal.hpp"
 
 namespace accspmm {
@@ -157,8 +158,7 @@ int spmm_host_impl(const accspmm_metcf_t* m, const accspmm_adpbme_t* ad, const f
 
     // C written by the kernel straight into host memory when it is pinned and
     // 16-byte aligned (the kernel stores float4s), else staged on the device
-    const char* direct_str = std::getenv("ACCSPMM_HOST_DIRECT");  // measurement override: 0 stages C
-    float* c_dev = (reinterpret_cast<uintptr_t>(C_host) & 15u) || (direct_str && std::atoi(direct_str) == 0)
+    float* c_dev = (reinterpret_cast<uintptr_t>(C_host) & 15u) || option(ACCSPMM_OPT_HOST_DIRECT_C) == 0
                        ? nullptr
                        : mapped_host(C_host);
     const bool direct = c_dev != nullptr;
@@ -179,10 +179,9 @@ int spmm_host_impl(const accspmm_metcf_t* m, const accspmm_adpbme_t* ad, const f
     } else if (ad) {
         // window offsets of the W real windows from rowIndices (windows past
         // W hold no tiles), the same derivation as accspmm_spmm_adaptive
-        HOST_CUDA(cudaMallocFromPoolAsync(&dR.p, (size_t(W) + 2) * 4, ctx->pool, s));
+        HOST_CUDA(cudaMallocFromPoolAsync(&dR.p, (size_t(W) + 1) * 4, ctx->pool, s));
         uint32_t* rw = static_cast<uint32_t*>(dR.p);
-        HOST_CUDA(cudaMemsetAsync(rw + W + 1, 0, 4, s));
-        r = rwo_from_row_indices(ad->row_indices, T, W, rw, rw + W + 1, s);
+        r = rwo_from_row_indices(ad->row_indices, T, W, rw, nullptr, true, s);
         if (r) return r;
         rwo = rw;
     }
@@ -196,9 +195,7 @@ int spmm_host_impl(const accspmm_metcf_t* m, const accspmm_adpbme_t* ad, const f
     uint32_t fs = slice_width_for(w_cfg, T, K, precision);
     fs = std::min(fs, std::max<uint32_t>(32u, (K / 4u) / 32u * 32u));
     if (fs > 64) fs = 64;
-    const char* fs_str = std::getenv("ACCSPMM_HOST_FS");  // measurement override
-    const int fs_env = fs_str ? std::atoi(fs_str) : 0;
-    if (fs_env == 32 || fs_env == 64 || fs_env == 128) fs = uint32_t(fs_env);
+    if (const int fs_opt = option(ACCSPMM_OPT_HOST_SLICE_WIDTH)) fs = uint32_t(fs_opt);
     const uint32_t nsl = (K + fs - 1) / fs;
     float* dBf = static_cast<float*>(dB.p);
 

@@ -51,10 +51,13 @@ int gather_floor_impl(const accspmm_metcf_t* m, const float* B, uint32_t K, uint
                       int repeats, float* avg_ms, void* stream);
 // Feature columns per slice the launch-shape chooser picks.
 uint32_t slice_width_for(uint32_t w_cfg, uint32_t T, uint32_t K, int precision);
-// rowWindowOffset of W windows derived from an AdpBME's rowIndices (err: a
-// word raised when rowIndices do not fit W windows or decrease).
+// rowWindowOffset of W windows derived from an AdpBME's rowIndices, with the
+// rowIndices checked on the way: bits raised when tiles lie past the W windows
+// (2) or rowIndices are not non-decreasing multiples of 8 (4) go to *err when
+// err is non-null (a zeroed device word) and, when `sticky`, to the device
+// status word that accspmm_device_status reports.
 int rwo_from_row_indices(const uint32_t* ri, uint32_t T, uint32_t W, uint32_t* rwo, uint32_t* err,
-                         cudaStream_t s);
+                         bool sticky, cudaStream_t s);
 int spmm_host_impl(const accspmm_metcf_t* m, const accspmm_adpbme_t* ad, const float* B_host,
                    float* C_host, uint32_t K, int precision, void* stream, int* direct_c);
 int spmm_bias_act_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K,

@@ -250,8 +250,8 @@ void accspmm_adpbme_destroy(accspmm_adpbme_t* adp);
  * stream order): the SpMM then gathers 10 instead of 16 sectors of each
  * 128-column row slice, with bit-identical results, and prefetches into L2
  * the rows of the tile group two ahead of the one it loads.
- * ACCSPMM_PACK=0 in the environment turns the packing off,
- * ACCSPMM_PREFETCH=0 the prefetch. */
+ * ACCSPMM_OPT_PACK and ACCSPMM_OPT_PREFETCH (accspmm_set_option) turn them
+ * off or on. */
 int accspmm_spmm_tf32(const accspmm_metcf_t* metcf, const float* B, float* C,
                       uint32_t K, int32_t precision, void* stream);
 
@@ -267,7 +267,16 @@ int accspmm_spmm_tf32(const accspmm_metcf_t* metcf, const float* B, float* C,
  * and waits for them on the host once, and must not be captured into a CUDA
  * graph (it returns ACCSPMM_ERROR_UNSUPPORTED inside a capture); later calls
  * may be captured.  For an AdpBME the caller filled they are derived into
- * stream-ordered scratch on every call.  B is packed as in accspmm_spmm_tf32. */
+ * stream-ordered scratch on every call.  B is packed as in accspmm_spmm_tf32.
+ * The derivation checks rowIndices: tiles whose window lies at or past
+ * c_rows / 8 (a c_rows below rowIndices.back() + 8, the reference's sizing
+ * rule, src/mma_tf32.cu:112) and rowIndices that are not non-decreasing
+ * multiples of 8 (include/format.hpp:364 writes each tile's window start).
+ * For a library-owned AdpBME the call returns ACCSPMM_ERROR_INVALID_VALUE
+ * (every call with that c_rows); for a caller-filled one the call is enqueued
+ * and accspmm_device_status reports ACCSPMM_ERROR_INVALID_VALUE afterwards
+ * (tiles past c_rows are then missing from C, misordered ones may be summed
+ * into the wrong windows; no read leaves the arrays). */
 int accspmm_spmm_adaptive(const accspmm_adpbme_t* adp, const float* B,
                           float* C, uint32_t c_rows, uint32_t K,
                           int32_t precision, void* stream);
@@ -337,10 +346,18 @@ int accspmm_spmm_host(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp,
  * process exits.  c_rows may be at most accspmm_noalloc_max_c_rows()
  * (8,388,592); larger sizes return ACCSPMM_ERROR_INVALID_VALUE.  The first
  * call on a device looks up the array's device address (cudaGetSymbolAddress)
- * and caches it; make that first call before any stream capture.  Every call
+ * and caches it for the life of the process; make that first call before any
+ * stream capture, and do not call this entry point after a cudaDeviceReset
+ * (the cached address belongs to the context the reset destroyed).  Every call
  * shares the one array and leaves the last call's contents in it, so calls
  * that overlap on the GPU (unordered streams) race; order them on one stream
- * or with events.  Same inputs, outputs and results as accspmm_spmm_adaptive. */
+ * or with events.  Same inputs and outputs as accspmm_spmm_adaptive and the
+ * same bits; rowIndices are checked in stream order and inconsistencies are
+ * reported by accspmm_device_status, as for a caller-filled AdpBME there.
+ * Unlike accspmm_spmm_adaptive it never packs B (the packed copy would need
+ * 320 cols ceil(K / 128) bytes of scratch): on a B of 128 MiB or more at
+ * K > 64 it runs the kernel that reads fp32 B, 2.29 against 1.95 ms per call
+ * on the 1M-row power-law matrix at K = 128 (GB300). */
 int accspmm_spmm_adaptive_noalloc(const accspmm_adpbme_t* adp, const float* B,
                                   float* C, uint32_t c_rows, uint32_t K,
                                   int32_t precision, void* stream);
@@ -354,7 +371,8 @@ int accspmm_time_spmm(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp,
                       int32_t precision, int32_t warmup, int32_t exe,
                       float* avg_ms, void* stream);
 
-/* Measurement: the gather floor of accspmm_spmm_tf32 on this matrix and B --
+/* Measurement build only (libaccspmm_lab.so; the product library returns
+ * ACCSPMM_ERROR_UNSUPPORTED): the gather floor of accspmm_spmm_tf32 on this matrix and B --
  * the average time (one warm-up, then `repeats` launches timed with CUDA
  * events on `stream`) of a kernel that moves exactly the B rows the SpMM
  * kernel gathers, with the SpMM's launch shape, lane pattern and batching
@@ -398,6 +416,58 @@ int accspmm_autotune_metcf(const accspmm_metcf_t* metcf, const float* B, float* 
                            accspmm_tune_result_t* result);
 /* Forgets every tuned shape. */
 void accspmm_autotune_clear(void);
+
+/* ---- options ------------------------------------------------------------- */
+/* Process-wide launch options.  No counterpart in the reference, whose launch
+ * shape is compiled in (include/tf32_comp.hpp:19-31, src/mma_tf32.cu:223).
+ * Each option starts from the environment variable named beside it, read
+ * once, at the first call that needs an option; afterwards only
+ * accspmm_set_option changes it, for every thread, from the next call on (a
+ * call already enqueued keeps the shape it was launched with).  Options change
+ * speed, not arithmetic: results are the same bits whatever they are set to,
+ * except ACCSPMM_OPT_WINDOWS_PER_CTA, which moves the boundaries at which
+ * partial row windows are summed (results then agree within the TF32
+ * tolerance).  accspmm_set_option returns ACCSPMM_ERROR_INVALID_VALUE for a
+ * value outside the listed ones, ACCSPMM_ERROR_UNSUPPORTED for a measurement
+ * kernel in a library built without them. */
+enum {
+    ACCSPMM_OPT_PACK = 0,             /* ACCSPMM_PACK (0 -> 0, 2 -> 1): -1 (default) TF32
+                                         launches at 128-column slices pack a B of at least
+                                         128 MiB to 2.5-byte TF32 rows first; 0 never; 1
+                                         whenever the launch shape allows */
+    ACCSPMM_OPT_PREFETCH = 1,         /* ACCSPMM_PREFETCH: 1 (default) the packed kernel
+                                         prefetches into L2 the rows of the tile group two
+                                         ahead; 0 it does not */
+    ACCSPMM_OPT_SCHEDULE = 2,         /* ACCSPMM_SCHEDULE: 1 (default) launches of a few
+                                         waves run their window blocks heaviest first; 0 in
+                                         window order */
+    ACCSPMM_OPT_SLICE_WIDTH = 3,      /* ACCSPMM_FS: 0 (default, the chooser's), 32, 64 or
+                                         128 feature columns per CTA */
+    ACCSPMM_OPT_CTAS_PER_SM = 4,      /* ACCSPMM_OCC: 0 (default), 2 or 3 */
+    ACCSPMM_OPT_TILE_RING = 5,        /* ACCSPMM_ROLL: -1 (default rule), 0 off, 1 on */
+    ACCSPMM_OPT_WINDOWS_PER_CTA = 6,  /* ACCSPMM_WB: 0 (default) or 1 .. 1024 */
+    ACCSPMM_OPT_HOST_SLICE_WIDTH = 7, /* ACCSPMM_HOST_FS: 0 (default), 32, 64 or 128
+                                         columns per accspmm_spmm_host slice */
+    ACCSPMM_OPT_HOST_DIRECT_C = 8,    /* ACCSPMM_HOST_DIRECT: 1 (default) the kernels store a
+                                         page-locked C_host straight over the host link; 0
+                                         stage it on the device */
+    ACCSPMM_OPT_KERNEL = 9            /* ACCSPMM_KERNEL (direct, pipe, bulk, lean, db, tma,
+                                         staged): 0 (default) the register-direct kernels;
+                                         the measurement variants 1 .. 6 exist only in the
+                                         measurement build, libaccspmm_lab.so */
+};
+/* values of ACCSPMM_OPT_KERNEL */
+enum {
+    ACCSPMM_KERNEL_DIRECT = 0,
+    ACCSPMM_KERNEL_PIPE = 1,   /* per-warp cp.async ring */
+    ACCSPMM_KERNEL_BULK = 2,   /* per-warp cp.async.bulk ring, one row per copy */
+    ACCSPMM_KERNEL_LEAN = 3,   /* register-direct at 64-80 registers a thread */
+    ACCSPMM_KERNEL_DB = 4,     /* double-buffered register-direct */
+    ACCSPMM_KERNEL_TMA = 5,    /* per-warp ring fed by tensor-map gather4 copies */
+    ACCSPMM_KERNEL_STAGED = 6  /* slice-major over B staged in 32-column TF32 slices */
+};
+int accspmm_set_option(int32_t option, int32_t value);
+int accspmm_get_option(int32_t option, int32_t* value);
 
 /* ---- batches ------------------------------------------------------------- */
 /* No counterpart in the reference (one matrix per process there).  A batch
@@ -479,10 +549,13 @@ int accspmm_server_reset_stats(accspmm_server_t* server);
 void accspmm_server_destroy(accspmm_server_t* server);
 
 /* Synchronises `stream`, then reports (and clears) the sticky status of the
- * SpMM kernels' bounded waits on the current device: ACCSPMM_ERROR_TIMEOUT if
- * a wait on an asynchronous copy expired since the last call (the affected
- * output rows are then undefined), else ACCSPMM_SUCCESS.  No counterpart in
- * the reference, whose kernels have no asynchronous-copy waits. */
+ * SpMM calls on the current device since the last report:
+ * ACCSPMM_ERROR_INVALID_VALUE if an adaptive call on a caller-filled AdpBME
+ * (accspmm_spmm_adaptive, _noalloc, accspmm_spmm_host) found rowIndices past
+ * its c_rows / 8 windows or not non-decreasing multiples of 8 (the message
+ * says which); ACCSPMM_ERROR_TIMEOUT if a bounded wait on an asynchronous copy
+ * expired (the affected output rows are then undefined); else
+ * ACCSPMM_SUCCESS.  No counterpart in the reference, which checks neither. */
 int accspmm_device_status(void* stream);
 
 /* Self-test of that failure path: launches one warp on `stream` that waits on

@@ -4,6 +4,8 @@ same inputs, whether C is written by the kernel straight into page-locked
 host memory or staged on the device and copied back (pageable or unaligned
 C), for the plain and the adaptive path, both precisions, and K that is not
 a multiple of the slice width."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -119,9 +121,14 @@ def test_argument_errors():
 
 
 def test_gather_floor_is_a_positive_time_below_the_spmm():
+    """The gather floor is a measurement entry point of libaccspmm_lab.so;
+    the product library refuses it."""
     m, cols = device_matrix("powerlaw40k")
     K = 128
     B = torch_dev(np.random.default_rng(3).uniform(-1, 1, (cols, K)).astype(np.float32))
+    ms = ctypes.c_float(0.0)
+    st = capi.load().accspmm_gather_floor(m.ref, ctypes.c_void_p(B.data_ptr()), K, 0, 3, ctypes.byref(ms), None)
+    assert st == capi.ERROR_UNSUPPORTED
     floor = m.gather_floor(B, K, 5)
     assert floor > 0
     for w in (32, 64, 128):

@@ -1,5 +1,6 @@
 """GPU parity: device builders bit-exact with the reference layout, SpMM within
 the stated tolerances of the oracle, all through the C ABI."""
+import ctypes
 import glob
 import os
 
@@ -150,9 +151,13 @@ def test_spmm_config1_against_csr_fp64():
 
 @pytest.mark.parametrize("name", ["longwin", "plsym1000", "rand203", "ragged_unsorted"])
 @pytest.mark.parametrize("prec", [capi.PREC_TF32, capi.PREC_3XTF32])
-def test_adaptive_equals_plain(name, prec):
+@pytest.mark.parametrize("K", [32, 36, 64, 128, 200, 256, 516])
+def test_adaptive_equals_plain(name, prec, K):
     """The adaptive entry point gives bit-identical rows to the plain one and
-    zeros in the extra rows of its larger C."""
+    zeros in the extra rows of its larger C, on both sides of the reference's
+    K = 128 switch between tf32_mma_balance_kernel and _g128_kernel
+    (include/tf32_comp.hpp:101-111) and at widths that are not multiples of
+    32 or of the 128-column slice."""
     g = gold(name)
     csr = csr_of_gold(g)
     m = device_metcf(csr)
@@ -160,7 +165,6 @@ def test_adaptive_equals_plain(name, prec):
     c_rows = a.c_rows()
     ah = a.to_numpy()
     assert c_rows == max(8 * (len(ah["group_offset"]) - 1), int(ah["row_indices"][-1]) + 8)
-    K = 64
     B = np.random.default_rng(1).uniform(-1, 1, (csr["cols"], K)).astype(np.float32)
     dB = torch_dev(B)
     dC = empty_dev(c_rows, K)
@@ -171,6 +175,37 @@ def test_adaptive_equals_plain(name, prec):
     n = min(c_rows, pl.shape[0])
     np.testing.assert_array_equal(ad[:n], pl[:n])
     assert not ad[n:].any()
+
+
+@pytest.mark.parametrize("name", ["plsym1000", "powerlaw40k"])
+@pytest.mark.parametrize("K", [256, 512])
+def test_adaptive_matches_oracle_above_k128(name, K):
+    """The adaptive path in the regime the reference serves with
+    tf32_mma_balance_g128_kernel (K > 128, include/mma_tf32.cuh:794-1042):
+    against the oracle's TF32 emulation (1e-5) and FP64 (1e-3), every row,
+    with zeros past the matrix's rows."""
+    if name == "powerlaw40k":
+        rp, ci, v = synth.powerlaw_local(n=40000, mean=16.0, d_max=1024, seed=5)
+        csr = dict(rows=40000, cols=40000, nnz=len(ci), row_ptr=rp, col_idx=ci, data=v)
+    else:
+        csr = csr_of_gold(gold(name))
+    m = device_metcf(csr)
+    h = m.to_numpy()
+    a = m.adpbme()
+    cr = a.c_rows()
+    B = np.random.default_rng(K + 1).uniform(-1, 1, (csr["cols"], K)).astype(np.float32)
+    dC = empty_dev(cr, K)
+    a.spmm(torch_dev(B), dC, cr, K)
+    torch.cuda.synchronize()
+    got = dC.cpu().numpy()
+    rows = 8 * m.struct.num_windows
+    emu = oracle.spmm_metcf_tf32(h, csr["cols"], B)
+    c64 = oracle.spmm_metcf_f64(h, csr["cols"], B)
+    assert np.isfinite(got).all()
+    assert rel_fro(got[:rows], emu) < TOL_TF32_VS_EMU
+    assert rel_fro(got[:rows], c64) < TOL_TF32_VS_F64
+    assert max_row_rel(got[:rows], c64) < 10 * TOL_TF32_VS_F64
+    assert not got[rows:].any()
 
 
 def test_spmm_deterministic():
@@ -313,7 +348,7 @@ def test_autotune_picks_a_shape_that_is_used_and_correct(K):
         capi.load().accspmm_autotune_clear()
 
 
-def test_heaviest_first_schedule_keeps_results_bitwise(monkeypatch):
+def test_heaviest_first_schedule_keeps_results_bitwise():
     """Launches of a few waves run their window blocks heaviest first; the
     schedule only changes which CTA runs a block, so plain and adaptive
     results are bitwise equal with and without it."""
@@ -326,12 +361,12 @@ def test_heaviest_first_schedule_keeps_results_bitwise(monkeypatch):
     B = torch.rand((n, K), device="cuda") * 2 - 1
     got = {}
     for sched in ("1", "0"):
-        monkeypatch.setenv("ACCSPMM_SCHEDULE", sched)
-        C = empty_dev(m.c_rows, K)
-        Ca = empty_dev(cr, K)
-        m.spmm(B, C, K)
-        a.spmm(B, Ca, cr, K)
-        torch.cuda.synchronize()
+        with capi.option(capi.OPT_SCHEDULE, int(sched)):
+            C = empty_dev(m.c_rows, K)
+            Ca = empty_dev(cr, K)
+            m.spmm(B, C, K)
+            a.spmm(B, Ca, cr, K)
+            torch.cuda.synchronize()
         got[sched] = (C, Ca)
     assert torch.equal(got["1"][0], got["0"][0])
     assert torch.equal(got["1"][1], got["0"][1])
@@ -406,14 +441,20 @@ def test_spmm_calls_capture_into_a_cuda_graph():
 
 
 @pytest.mark.parametrize("prec", [capi.PREC_TF32, capi.PREC_3XTF32])
-@pytest.mark.parametrize("kernel", ["pipe", "bulk", "tma", "lean", "db"])
+@pytest.mark.parametrize("kernel", ["pipe", "bulk", "tma", "lean", "db", "staged"])
 @pytest.mark.parametrize("name,K", [("plsym1000", 32), ("plsym1000", 128), ("longwin", 64)])
-def test_measurement_kernel_variants(monkeypatch, kernel, name, K, prec):
-    """The kernel variants kept for measurement (ACCSPMM_KERNEL) compute the
-    same product: bitwise equal to the default register-direct kernel where
-    they cut the window blocks among the same 8 warps (lean, db), within the
-    TF32 emulation tolerance where they use 4 warps per CTA (pipe, bulk,
-    tma: their warps' pieces, and so the partial-window sums, differ)."""
+def test_measurement_kernel_variants(kernel, name, K, prec):
+    """The kernel variants kept for measurement in libaccspmm_lab.so
+    (ACCSPMM_OPT_KERNEL) compute the same product: bitwise equal to the
+    product library's register-direct kernel where they cut the window blocks
+    among the same 8 warps (lean, db, staged), within the TF32 emulation
+    tolerance where they use 4 warps per CTA (pipe, bulk, tma: their warps'
+    pieces, and so the partial-window sums, differ).  The product library
+    refuses the variants."""
+    lab = capi.load_lab()
+    with pytest.raises(capi.AccSpmmError) as e:
+        capi.set_option(capi.OPT_KERNEL, capi.KERNELS[kernel])
+    assert e.value.status == capi.ERROR_UNSUPPORTED
     g = gold(name)
     csr = csr_of_gold(g)
     m = device_metcf(csr)
@@ -422,12 +463,13 @@ def test_measurement_kernel_variants(monkeypatch, kernel, name, K, prec):
     dB = torch_dev(B)
     C0 = empty_dev(m.c_rows, K)
     m.spmm(dB, C0, K, prec)
-    monkeypatch.setenv("ACCSPMM_KERNEL", kernel)
     C1 = empty_dev(m.c_rows, K)
-    m.spmm(dB, C1, K, prec)
+    with capi.option(capi.OPT_KERNEL, capi.KERNELS[kernel], lib=lab):
+        capi.call_lab("accspmm_spmm_tf32", m.ref, ctypes.c_void_p(dB.data_ptr()),
+                      ctypes.c_void_p(C1.data_ptr()), K, prec, None)
     torch.cuda.synchronize()
-    capi.call("accspmm_device_status", None)  # raises if a bounded wait expired
-    if kernel in ("lean", "db"):
+    capi.call_lab("accspmm_device_status", None)  # raises if a bounded wait expired
+    if kernel in ("lean", "db", "staged"):
         assert torch.equal(C0, C1)
     got = C1.cpu().numpy()
     f64 = oracle.spmm_metcf_f64(h, csr["cols"], B)
@@ -579,7 +621,7 @@ def test_device_builders_match_the_oracle_at_full_size():
 
 
 @pytest.mark.slow
-def test_packed_b_with_prefetch_is_bit_identical_at_full_size(monkeypatch):
+def test_packed_b_with_prefetch_is_bit_identical_at_full_size():
     """On the 1M-row power-law matrix (seed 0, K = 128, a 512 MB B) the packed
     kernel returns the same bits with its L2 prefetch of the rows two tile
     groups ahead (the default), without it (ACCSPMM_PREFETCH=0), and reading
@@ -593,12 +635,11 @@ def test_packed_b_with_prefetch_is_bit_identical_at_full_size(monkeypatch):
     dB = torch.rand((n, K), device="cuda", generator=torch.Generator(device="cuda").manual_seed(0)) * 2 - 1
     out = {}
     for pf, pk in (("1", "1"), ("0", "1"), ("1", "0")):
-        monkeypatch.setenv("ACCSPMM_PREFETCH", pf)
-        monkeypatch.setenv("ACCSPMM_PACK", pk)
-        C, Ca = empty_dev(m.c_rows, K), empty_dev(cr, K)
-        m.spmm(dB, C, K)
-        a.spmm(dB, Ca, cr, K)
-        torch.cuda.synchronize()
+        with capi.option(capi.OPT_PREFETCH, int(pf)), capi.option(capi.OPT_PACK, -1 if pk == "1" else 0):
+            C, Ca = empty_dev(m.c_rows, K), empty_dev(cr, K)
+            m.spmm(dB, C, K)
+            a.spmm(dB, Ca, cr, K)
+            torch.cuda.synchronize()
         out[pf + pk] = (C, Ca)
     for key in ("01", "10"):
         assert torch.equal(out["11"][0], out[key][0]), key
@@ -607,7 +648,7 @@ def test_packed_b_with_prefetch_is_bit_identical_at_full_size(monkeypatch):
 
 
 @pytest.mark.parametrize("K", [136, 256])
-def test_packed_b_is_bit_identical(monkeypatch, K):
+def test_packed_b_is_bit_identical(K):
     """TF32 launches at 128-column slices whose B is at least 128 MiB first
     pack B to 2.5 bytes a value (rounded to TF32; each 128-column slice of a
     row its halfwords of bits 31..16, then the nibbles of bits 15..12); the
@@ -623,11 +664,11 @@ def test_packed_b_is_bit_identical(monkeypatch, K):
     dB = torch.rand((n, K), device="cuda") * 2 - 1
     out = {}
     for pk in ("1", "0"):
-        monkeypatch.setenv("ACCSPMM_PACK", pk)
-        C, Ca = empty_dev(m.c_rows, K), empty_dev(cr, K)
-        m.spmm(dB, C, K)
-        a.spmm(dB, Ca, cr, K)
-        torch.cuda.synchronize()
+        with capi.option(capi.OPT_PACK, -1 if pk == "1" else 0):
+            C, Ca = empty_dev(m.c_rows, K), empty_dev(cr, K)
+            m.spmm(dB, C, K)
+            a.spmm(dB, Ca, cr, K)
+            torch.cuda.synchronize()
         out[pk] = (C, Ca)
     assert torch.equal(out["1"][0], out["0"][0]) and torch.equal(out["1"][1], out["0"][1])
     rows = np.sort(np.random.default_rng(K).choice(n, 2048, replace=False))
@@ -641,8 +682,8 @@ def test_packed_b_is_bit_identical(monkeypatch, K):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("K", [72, 128, 200])
-def test_forced_packing_on_a_small_b_is_bit_identical(monkeypatch, K):
-    """ACCSPMM_PACK=2 packs B wherever the launch shape allows, also below the
+def test_forced_packing_on_a_small_b_is_bit_identical(K):
+    """ACCSPMM_OPT_PACK = 1 packs B wherever the launch shape allows, also below the
     default rule's 128 MiB: ragged last slices (K = 72, 200), rows that are
     not a multiple of the window height, the plain and adaptive entry points."""
     n = 5003
@@ -654,11 +695,11 @@ def test_forced_packing_on_a_small_b_is_bit_identical(monkeypatch, K):
     dB = torch.rand((n, K), device="cuda") * 2 - 1
     out = {}
     for pk in ("2", "0"):
-        monkeypatch.setenv("ACCSPMM_PACK", pk)
-        C, Ca = empty_dev(m.c_rows, K), empty_dev(cr, K)
-        m.spmm(dB, C, K)
-        a.spmm(dB, Ca, cr, K)
-        torch.cuda.synchronize()
+        with capi.option(capi.OPT_PACK, 1 if pk == "2" else 0):
+            C, Ca = empty_dev(m.c_rows, K), empty_dev(cr, K)
+            m.spmm(dB, C, K)
+            a.spmm(dB, Ca, cr, K)
+            torch.cuda.synchronize()
         out[pk] = (C, Ca)
     assert torch.equal(out["2"][0], out["0"][0]) and torch.equal(out["2"][1], out["0"][1])
     ref = oracle.spmm_csr_f64(rp, ci, vals, dB.cpu().numpy())
