@@ -61,14 +61,14 @@ __global__ void __launch_bounds__(NW * 32, MINB) spmm_window_kernel(const SpmmAr
 // The register-direct kernel with the rolling ring reading B from its packed
 // TF32 rows (a.bp): bit-identical to spmm_window_kernel<FS, TF32, U,
 // MINB, false, NW, true>, with a quarter fewer gathered sectors.
-template <int FS, int U, int MINB, int NW = kNW, bool PF = false>
+template <int FS, int U, int MINB, int NW = kNW, bool PF = false, int PFK = 2>
 __global__ void __launch_bounds__(NW * 32, MINB) spmm_window_packed_kernel(const SpmmArgs a) {
     extern __shared__ __align__(16) float smem[];
     float* part = smem;  // [2 * NW] slots
     uint32_t* s_rwo = reinterpret_cast<uint32_t*>(smem + 2 * NW * 8 * FS);
     Block<FS, NW> blk;
     blk.init(a, s_rwo, part);
-    direct_item_packed<FS, U, NW, PF>(a, blk);
+    direct_item_packed<FS, U, NW, PF, PFK>(a, blk);
 }
 
 // B rounded to TF32 (cvt.rna, as the SpMM's operands are) and packed row by
@@ -603,21 +603,21 @@ int launch_direct(const SpmmArgs& a, int occ, int ring, cudaStream_t s) {
     return epi ? launch_direct_t<FS, PREC, U, 2, true>(a, s) : launch_direct_t<FS, PREC, U, 2, false>(a, s);
 }
 
-template <int FS, int U, int MINB, bool PF = false>
+template <int FS, int U, int MINB, bool PF = false, int PFK = 2>
 int launch_packed_t(const SpmmArgs& a, cudaStream_t s) {
     const size_t smem = size_t(2 * kNW * 8 * FS) * 4 + size_t(a.wb + 1) * 4;
     static unsigned attr_set = 0;  // one bit per device
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 32 && !(attr_set & (1u << dev))) {
-        ACC_CUDA(cudaFuncSetAttribute(spmm_window_packed_kernel<FS, U, MINB, kNW, PF>,
+        ACC_CUDA(cudaFuncSetAttribute(spmm_window_packed_kernel<FS, U, MINB, kNW, PF, PFK>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
         attr_set |= 1u << dev;
     }
     const uint64_t grid = uint64_t(a.n_wblocks) * a.n_slices;
     if (grid == 0) return ACCSPMM_SUCCESS;
     if (grid > 0x7FFFFFFFull) ACC_FAIL(ACCSPMM_ERROR_OVERFLOW, "grid too large");
-    spmm_window_packed_kernel<FS, U, MINB, kNW, PF><<<unsigned(grid), kNW * 32, smem, s>>>(a);
+    spmm_window_packed_kernel<FS, U, MINB, kNW, PF, PFK><<<unsigned(grid), kNW * 32, smem, s>>>(a);
     ACC_LAUNCH_CHECK();
     return ACCSPMM_SUCCESS;
 }
@@ -773,9 +773,15 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
         // the B rows of the tile group two ahead are prefetched into L2
         // (ACCSPMM_OPT_PREFETCH = 0 turns it off): 1.99 against 2.06 ms per
         // step at K = 128, 3.82 against 4.01 ms at K = 256, bit-identical
-        if (st == ACCSPMM_SUCCESS)
+        if (st == ACCSPMM_SUCCESS) {
+#ifdef ACCSPMM_LAB
+            if (option(ACCSPMM_OPT_PREFETCH) && lab_env("ACCSPMM_PFK", 2) == 1)
+                st = launch_packed_t<128, DirectBatch<128>::U, 2, true, 1>(a, s);
+            else
+#endif
             st = option(ACCSPMM_OPT_PREFETCH) ? launch_packed_t<128, DirectBatch<128>::U, 2, true>(a, s)
                                               : launch_packed_t<128, DirectBatch<128>::U, 2>(a, s);
+        }
         cudaFreeAsync(packed, s);
         if (st) ACC_FAIL(st, "packed SpMM launch failed");
         return ACCSPMM_SUCCESS;

@@ -178,7 +178,11 @@ __device__ __forceinline__ void direct_item(const SpmmArgs& a, const Block<FS, N
 // whose products land only in columns that are not stored): 8 % fewer
 // instructions and 5 % less time than predicated loads on the 1M-row
 // power-law matrix at K = 128 and 256.
-template <int FS, int U, int NW = kDirectNW, bool PF = false>
+// PFK: how rows are prefetched -- 1 one cp.async.bulk.prefetch.L2 of the
+// 320-byte slice per row (its address operand is uniform, so the lanes'
+// prefetches issue one after another), 2 three prefetch.global.L2 of the
+// slice's 128-byte lines per row, issued by the lanes together.
+template <int FS, int U, int NW = kDirectNW, bool PF = false, int PFK = 2>
 __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Block<FS, NW>& blk) {
     constexpr int H = FS / 32;
     using L = Layout<H>;
@@ -255,7 +259,14 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
         auto prefetch_rows = [&]() {
             if (PF && lane >= 8 * U && ma[0] < a.cols) {
                 const uint8_t* r = a.bp + size_t(ma[0]) * a.bpitch + 320 * (blk.f0 / 128);
-                asm volatile("cp.async.bulk.prefetch.L2.global [%0], 320;" ::"l"(r) : "memory");
+                if (PFK == 1) {
+                    asm volatile("cp.async.bulk.prefetch.L2.global [%0], 320;" ::"l"(r) : "memory");
+                } else {
+                    // the three 128-byte lines that hold the 320-byte slice
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(r));
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(r + 128));
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(r + 256));
+                }
             }
         };
 #pragma unroll

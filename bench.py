@@ -69,6 +69,14 @@ def parse():
     p.add_argument("--rows-hi", type=int, default=0,
                    help="largest graph rows of the batch / serve workloads (default: the "
                         "stated 200,000 for batch, 500,000 for serve)")
+    p.add_argument("--rates", default="100,500,1000,2000,5000",
+                   help="serve workload: offered request rates (req/s), comma-separated")
+    p.add_argument("--no-extras", action="store_true",
+                   help="scale workload: skip the compact runs of the small, precision, batch "
+                        "and serve workloads added to the line under `extra`")
+    p.add_argument("--profile-step", type=int, default=0, metavar="STEPS",
+                   help="scale workload: build, then run STEPS timed-path steps (default launch "
+                        "shape, no timing) and exit: the command whose DRAM bytes ncu records")
     p.add_argument("--profile", type=int, default=0, metavar="LAUNCHES",
                    help="only build METCF on the GPU and run LAUNCHES plain SpMM launches "
                         "(no timing): the command profiled by ncu")
@@ -157,11 +165,13 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def algorithmic_bytes(nnz, T, W, cols, K, G=None):
+def algorithmic_bytes(nnz, T, W, cols, K, G=None, c_rows=None):
     """Compulsory traffic of one SpMM: values, bitmaps, tcOffset, sparseA2B,
-    rowWindowOffset, B read once, C written once (+ AdpBME row indices and
-    group offsets on the adaptive path)."""
-    b = 4 * nnz + 8 * T + 4 * (T + 1) + 32 * T + 4 * (W + 1) + 4 * cols * K + 4 * 8 * W * K
+    rowWindowOffset, B read once, C written once (8W rows on the plain path;
+    on the adaptive path the caller's c_rows, plus AdpBME row indices and
+    group offsets)."""
+    rows_c = 8 * W if c_rows is None else c_rows
+    b = 4 * nnz + 8 * T + 4 * (T + 1) + 32 * T + 4 * (W + 1) + 4 * cols * K + 4 * rows_c * K
     if G is not None:
         b += 4 * T + 4 * (G + 1)
     return b
@@ -176,18 +186,38 @@ def peaks():
         return 6800.0, "fallback"
 
 
+# DRAM bytes of one adaptive step (the B-packing launch and the SpMM launch)
+# on the 1M-row workload, from one ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum, one pass, --clock-control none) of
+# `bench.py --profile-step 3 --no-autotune` at that K; keyed with the hash of
+# the kernel sources it was captured on, so that the figure is reported only
+# while those sources are unchanged (a stale figure is reported as null, with
+# the reason).
+KERNEL_SOURCES = ("accspmm_gb300/csrc/spmm.cu", "accspmm_gb300/csrc/spmm_direct.cuh",
+                  "accspmm_gb300/csrc/spmm_common.cuh")
+TRAFFIC = {}
+
+
+def kernel_source_hash():
+    import hashlib
+    h = hashlib.sha256()
+    for rel in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, rel), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
+
+
 def measured_traffic(K):
-    """DRAM bytes per launch of the SpMM kernel from the committed ncu summary
-    (profiles/spmm_window_kernel_powerlaw_local.md), if one exists for K."""
-    path = os.path.join(ROOT, "profiles", "spmm_window_kernel_powerlaw_local.md")
-    try:
-        with open(path) as f:
-            for line in f:
-                if line.startswith(f"traffic_bytes_per_launch K={K}:"):
-                    return int(line.split(":", 1)[1].strip())
-    except OSError:
-        pass
-    return None
+    """(bytes per step, source) of the last ncu capture at K, or (None,
+    why) when there is none or the kernel sources changed since."""
+    t = TRAFFIC.get(K)
+    if t is None:
+        return None, f"no ncu capture at K={K}"
+    cur = kernel_source_hash()
+    if cur != t["src_sha"]:
+        return None, (f"stale: ncu capture {t['capture']} was taken on kernel sources {t['src_sha']}, "
+                      f"these are {cur}")
+    return t["bytes"], f"ncu {t['capture']} (kernel sources {cur})"
 
 
 def replica_throughput(ms: float, flops_per_step: float, world: int, device=None):
@@ -254,6 +284,22 @@ def cpu_baseline(rp, ci, v, B, budget_s=8.0):
                       f"FP32 CSR SpMM, OpenMP over rows"}
 
 
+def scale_config(n, K, nnz, rp, T, W, G, seed):
+    """The workload's identity, printed identically by both arms."""
+    return {"workload": workload_name(n, K), "n_rows": n, "nnz": nnz, "K": K,
+            "realised_degree": degree_stats(rp), "tiles": int(T), "windows": int(W),
+            "groups": None if G is None else int(G), "seed": seed,
+            "l2": "no flush: B (N*K*4 bytes) and METCF exceed the 129 MB L2"}
+
+
+def small_config(n, K, nnz, rp, T, W, G):
+    """The 16,384-row workload's identity, printed identically by both arms."""
+    return {"workload": small_workload_name(K), "n_rows": n, "nnz": nnz, "K": K,
+            "tiles": int(T), "windows": int(W), "groups": None if G is None else int(G),
+            "realised_degree": degree_stats(rp),
+            "l2": "flushed before every timed step (256 MB written)"}
+
+
 def small_workload(seed: int):
     """The 16,384-row symmetric power-law matrix (full symmetric COO)."""
     from accspmm_gb300 import synth
@@ -274,14 +320,22 @@ def run_reference(args):
         r, c, vv = small_workload(args.seed)
         args.n = 16384
         rp, ci, v = oracle.csr_from_coo(args.n, r, c, vv)
-        wname = small_workload_name(args.k)
     elif args.workload == "scale":
         rp, ci, v = workload(args.n, args.seed)
-        wname = workload_name(args.n, args.k)
     else:
         print(json.dumps({"impl": "reference", "unavailable": f"no reference arm for the {args.workload} "
                           "workload (the reference has no batched or served path)"}))
         return
+    # the METCF / AdpBME shape of the matrix (the oracle's restatement of the
+    # reference's builders), for the config both arms print
+    mref = oracle.metcf(args.n, rp, ci, v)
+    adaptive = bool(oracle.balance_strategy(mref["rwo"]))
+    n_groups = len(oracle.adpbme_groups(mref["rwo"])) - 1 if adaptive else None
+    T, W = len(mref["tc_offset"]) - 1, len(mref["rwo"]) - 1
+    if args.workload == "small":
+        config = small_config(args.n, args.k, int(len(ci)), rp, T, W, n_groups)
+    else:
+        config = scale_config(args.n, args.k, int(len(ci)), rp, T, W, n_groups, args.seed)
     B = np.random.default_rng(args.seed + 7).uniform(-1, 1, (args.n, args.k)).astype(np.float32)
     threads = oracle.omp_max_threads()
     C = np.zeros((args.n, args.k), np.float32)
@@ -314,20 +368,19 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
         "data": "synthetic", "impl": "reference",
-        "config": {"workload": wname, "n_rows": args.n, "nnz": int(len(ci)),
-                   "realised_degree": degree_stats(rp),
-                   "K": args.k, "path": "CPU CSR SpMM (oracle port; the reference has no CPU SpMM)"},
+        "config": config,
+        "run": {"path": "CPU CSR SpMM (oracle port; the reference has no CPU SpMM)"},
         "cpu_baseline": {"value": round(gf, 2), "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{rows_per_step} consecutive rows per step (of {args.n}), "
                                    f"{args.steps} steps"},
         "e2e": {"value": round(gf, 2), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     if not args.no_ref_gpu:
-        out["reference_gpu_kernels"] = reference_gpu(args, rp, ci, v)
+        out["reference_gpu_kernels"] = reference_gpu(args, rp, ci, v, mref)
     print(json.dumps(out))
 
 
-def reference_gpu(args, rp, ci, v):
+def reference_gpu(args, rp, ci, v, m):
     """The reference's own SpMM kernels (include/mma_tf32.cuh compiled for
     sm_103a from its sources) on this GPU, on the same matrix, timed with the
     reference's method: the kernel its driver picks for the matrix (the
@@ -340,7 +393,6 @@ def reference_gpu(args, rp, ci, v):
         return {"unavailable": why}
     import torch
     n, nnz = args.n, int(len(ci))
-    m = oracle.metcf(n, rp, ci, v)
     adaptive = bool(oracle.balance_strategy(m["rwo"]))
     groups = oracle.adpbme_groups(m["rwo"]) if adaptive else None
     ri = oracle.adpbme_row_indices(m["rwo"]) if adaptive else None
@@ -435,6 +487,13 @@ def run_ours(args):
     B = torch.rand((n, K), device=dev, generator=gen) * 2 - 1
     C = torch.empty((c_rows, K), device=dev)
 
+    if args.profile_step:
+        for _ in range(args.profile_step):
+            (adp.spmm(B, C, c_rows, K, prec, stream) if adaptive else m.spmm(B, C, K, prec, stream))
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_steps": args.profile_step, "K": K, "tiles": int(T),
+                          "path": "adaptive" if adaptive else "plain"}))
+        return
     tune = None
     if not args.no_autotune:
         # pick the launch shape for this matrix once, before anything is timed
@@ -488,31 +547,25 @@ def run_ours(args):
     accuracy = {"rel_fro_vs_fp64": fp64_error(C, B),
                 "reference": "torch sparse CSR matmul in float64 on the GPU"}
 
-    # the dominant kernel: one call of the plain entry point (the SpMM launch,
-    # with the B-packing launch before it where that applies: both timed)
-    for _ in range(3):
-        m.spmm(B, C, K, prec, stream)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    reps = 10
-    for _ in range(reps):
-        m.spmm(B, C, K, prec, stream)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    kms = e0.elapsed_time(e1) / reps
-    abytes = algorithmic_bytes(nnz, T, W, n, K)
+    # roofline of the timed step (the B-packing launch, where it applies, and
+    # the SpMM launch, which takes about nine tenths of it): the step's
+    # compulsory bytes over the step time measured above
+    kms = ms
+    abytes = algorithmic_bytes(nnz, T, W, n, K, G, c_rows if adaptive else None)
     achieved = abytes / (kms * 1e-3) / 1e9
     peak, peak_kind = peaks()
-    traffic = measured_traffic(K)
+    traffic, traffic_source = measured_traffic(K) if (n == 1 << 20 and args.seed == 0) else \
+        (None, "ncu captures exist for the 1M-row workload with seed 0 only")
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": traffic,
+                "frac": round(achieved / peak, 4), "traffic": traffic, "traffic_source": traffic_source,
                 "peak_source": f"{peak_kind} hbm_gbs",
                 "kernel": ("pack_tf32_kernel + spmm_window_packed_kernel" if launches_per_step == 2
                            else "spmm_window_kernel"),
-                "kernel_ms": round(kms, 4), "algorithmic_bytes": int(abytes)}
+                "kernel_ms": round(kms, 4), "algorithmic_bytes": int(abytes),
+                "timing": "the timed region's steps (CUDA events on the launching stream)"}
     if traffic:
-        # the DRAM bytes the kernel really moves (ncu, per launch) over its
-        # live time: achieved HBM bandwidth, against the same measured peak
+        # the DRAM bytes the step really moves (ncu) over its live time:
+        # achieved HBM bandwidth, against the same measured peak
         roofline["dram_gbs"] = round(traffic / (kms * 1e-3) / 1e9, 1)
         roofline["dram_frac"] = round(traffic / (kms * 1e-3) / 1e9 / peak, 4)
     # gather model (diagnostic): B counted as one K-float row per non-padding
@@ -576,8 +629,10 @@ def run_ours(args):
             e1.record(stream)
             torch.cuda.synchronize()
             kt = e0.elapsed_time(e1) / 10
+            kb = algorithmic_bytes(nnz, T, W, n, kk, G, c_rows if adaptive else None)
             sweep[str(kk)] = {"ms": round(kt, 4), "gflops": round(2.0 * nnz * kk / (kt * 1e-3) / 1e9, 1),
-                              "gbs_algorithmic": round(algorithmic_bytes(nnz, T, W, n, kk) / (kt * 1e-3) / 1e9, 1)}
+                              "gbs_algorithmic": round(kb / (kt * 1e-3) / 1e9, 1),
+                              "rel_fro_vs_fp64": fp64_error(Ck, Bk)}
             del Bk, Ck
 
     cusparse = None
@@ -591,21 +646,22 @@ def run_ours(args):
     if not args.no_cpu_baseline:
         Bnp = B[:, :].cpu().numpy()
         cpu = cpu_baseline(rp, ci, vals, Bnp)
+    extra = None
+    if world == 1 and not args.no_extras:
+        del B, C
+        torch.cuda.empty_cache()
+        extra = run_extras(args)
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": args.precision, "data": "synthetic",
-        "config": {"workload": workload_name(n, K), "n_rows": n, "nnz": nnz, "K": K,
-                   "realised_degree": degree_stats(rp),
-                   "tiles": int(T), "windows": int(W), "groups": G,
-                   "path": "adaptive" if adaptive else "plain",
-                   "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": "no flush: B (N*K*4 bytes) and METCF exceed the 129 MB L2",
-                   "metcf_build_ms": {"device": round(device_build_ms, 1),
-                                      "host": round(host_build_ms, 1) if host_build_ms else None},
-                   "seed": args.seed,
-                   "launch_shape": tune or "default"},
+        "config": scale_config(n, K, nnz, rp, T, W, G, args.seed),
+        "run": {"path": "adaptive" if adaptive else "plain",
+                "parallelism": "replicas" if world > 1 else "single GPU",
+                "metcf_build_ms": {"device": round(device_build_ms, 1),
+                                   "host": round(host_build_ms, 1) if host_build_ms else None},
+                "launch_shape": tune or "default"},
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
@@ -614,10 +670,74 @@ def run_ours(args):
         "clocks": clk.summary(),
         "k_sweep": sweep,
         "comparators": {"cusparse_csr": cusparse},
+        "extra": extra,
     }
     print(json.dumps(out))
     if world > 1:
         dist.destroy_process_group()
+
+
+def run_extras(args):
+    """The other workloads, each in a child process of its own (so that its
+    device memory is returned when it ends) with short timed loops, reduced
+    to the keys that state their result: the 16,384-row matrix with and
+    without L2 flushes, TF32 against 3xTF32 against FP64 on the 2M-row GCN
+    graph, the 512-graph batch against separate launches, and the server at
+    one offered rate below and one above the saturation of one request per
+    launch.  A workload that fails or runs out of time is reported as such."""
+    me = os.path.abspath(__file__)
+    runs = {
+        "small": (["--workload", "small", "--steps", "50", "--warmup", "5", "--no-cpu-baseline"], 120),
+        "precision": (["--workload", "precision"], 300),
+        "batch": (["--workload", "batch", "--steps", "5", "--warmup", "3"], 400),
+        "serve": (["--workload", "serve", "--rates", "500,2000"], 400),
+    }
+    out = {}
+    for name, (argv, limit) in runs.items():
+        t0 = time.perf_counter()
+        try:
+            r = subprocess.run([sys.executable, me, *argv, "--seed", str(args.seed)], capture_output=True,
+                               text=True, timeout=limit)
+            lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+            if r.returncode != 0 or not lines:
+                out[name] = {"failed": f"exit {r.returncode}: {r.stderr.strip().splitlines()[-1:]}"}
+                continue
+            d = json.loads(lines[-1])
+        except subprocess.TimeoutExpired:
+            out[name] = {"failed": f"ran past {limit} s"}
+            continue
+        wall = round(time.perf_counter() - t0, 1)
+        if name == "small":
+            out[name] = {"workload": d["config"]["workload"], "K": d["config"]["K"],
+                         "flushed_us": round(d["ms_per_step"] * 1e3, 2),
+                         "back_to_back_us": round(d["no_flush"]["ms_per_step"] * 1e3, 2),
+                         "gflops_flushed": d["value"], "gflops_back_to_back": d["no_flush"]["value"],
+                         "path": d["run"]["path"], "wall_s": wall}
+        elif name == "precision":
+            p = d["precision"]
+            out[name] = {"workload": d["config"]["workload"],
+                         "tf32": {k: p["tf32"][k] for k in ("ms", "rel_fro", "max_row_rel")},
+                         "3xtf32": {k: p["3xtf32"][k] for k in ("ms", "rel_fro", "max_row_rel")},
+                         "time_ratio_3xtf32_over_tf32": d["time_ratio_3xtf32_over_tf32"],
+                         "targets": d["targets"], "wall_s": wall}
+        elif name == "batch":
+            b = d["batch"]
+            out[name] = {"workload": d["config"]["workload"], "graphs": d["config"]["graphs"],
+                         "graph_replay_ms": b["graph_replay_ms"],
+                         "separate_launches_ms": b["separate_launches_ms"],
+                         "speedup_vs_separate": b["speedup_vs_separate"],
+                         "bitwise_equal_to_separate": b["bitwise_equal_to_separate"],
+                         "rel_fro_vs_fp64_max": b["rel_fro_vs_fp64_max"], "wall_s": wall}
+        else:
+            sv = d["serve"]
+            out[name] = {"workload": d["config"]["workload"],
+                         "by_offered_rps": {rate: {mode: {k: sv[mode][rate][k] for k in
+                                                          ("achieved_rps", "p50_ms", "p99_ms")}
+                                                   for mode in sv} for rate in sv["per_request"]},
+                         "served_error": {k: d["served_error"][k] for k in
+                                          ("rel_fro_vs_fp64_max", "samples", "two_layer_chains")},
+                         "precision": d["dtype"], "wall_s": wall}
+    return out
 
 
 def run_small(args):
@@ -694,11 +814,8 @@ def run_small(args):
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(cold_ms, 5),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": args.precision, "data": "synthetic",
-        "config": {"workload": small_workload_name(K),
-                   "n_rows": n, "nnz": nnz, "K": K, "tiles": int(T), "windows": int(W), "groups": G,
-                   "realised_degree": degree_stats(csr["row_ptr"]),
-                   "path": "adaptive" if adaptive else "plain",
-                   "l2": "flushed before every timed step (256 MB written)"},
+        "config": small_config(n, K, nnz, csr["row_ptr"], T, W, G),
+        "run": {"path": "adaptive" if adaptive else "plain"},
         "no_flush": {"ms_per_step": round(warm_ms, 5),
                      "value": round(flops / (warm_ms * 1e-3) / 1e9, 2),
                      "timing": "back-to-back launches, one event pair around the loop"},
@@ -994,7 +1111,7 @@ def run_serve(args):
 
     budget = 150 * (1 << 30)
     results = {}
-    rates = [100, 500, 1000, 2000, 5000]
+    rates = [int(r) for r in args.rates.split(",") if r.strip()]
     for name, mb, ns in (("continuous_batching", 64, 4), ("per_request", 1, 1)):
         srv = api.Server(graphs, budget, max_batch=mb, streams=ns)
         drive(srv, 200, 50)  # warm-up
