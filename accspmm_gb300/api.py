@@ -199,6 +199,14 @@ def permute_rows(src, dst, idx, rows: int, K: int, scatter: bool = False, stream
          C.c_void_p(_addr(idx)), rows, K, 1 if scatter else 0, _stream(stream))
 
 
+def dense_matmul(H, n: int, k_in: int, W, k_out: int, XW, precision: int = capi.PREC_TF32,
+                 stream=None) -> None:
+    """XW = H W on the device (accspmm_dense_matmul): H n x k_in, W k_in x
+    k_out, XW n x k_out, row-major fp32, on the tcgen05 tensor cores."""
+    call("accspmm_dense_matmul", C.c_void_p(_addr(H)), n, k_in, C.c_void_p(_addr(W)), k_out,
+         C.c_void_p(_addr(XW)), precision, _stream(stream))
+
+
 def save_metcf(m: dict, path: str) -> None:
     """Writes a host METCF (dict of arrays) to a binary file."""
     k = metcf_struct(m)
@@ -371,7 +379,8 @@ class DeviceMETCF(DeviceObject):
     def gcn_layer(self, H, k_in: int, W, k_out: int, out, bias=None,
                   activation: int = capi.ACT_RELU, precision: int = capi.PREC_TF32,
                   stream=None) -> None:
-        """out = act(A * (H W) + bias): cuBLAS for H W, the fused SpMM for A."""
+        """out = act(A * (H W) + bias): the tcgen05 GEMM for H W, the fused
+        SpMM for A."""
         call("accspmm_gcn_layer", self.ref, C.c_void_p(_addr(H)), k_in, C.c_void_p(_addr(W)),
              k_out, C.c_void_p(_addr(bias)), activation, C.c_void_p(_addr(out)), precision,
              _stream(stream))

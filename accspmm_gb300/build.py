@@ -28,7 +28,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # the product library
 LIB_UNITS = ["host_formats.cpp", "metcf_io.cpp", "reorder.cpp", "permute.cu", "capi.cpp", "options.cpp",
              "device_prims.cu", "metcf_device.cu", "spmm.cu", "spmm_host.cpp", "spmm_batch.cu",
-             "server.cpp", "gnn.cpp"]
+             "server.cpp", "gnn.cpp", "dense_gemm.cu"]
 # the measurement build (libaccspmm_lab.so, -DACCSPMM_LAB): the same units plus
 # the variant kernels kept for measurement (cp.async / bulk / tensor-map rings,
 # lean, double-buffered, slice-major over staged B) and the gather floor
@@ -85,7 +85,7 @@ def _link(out: str, objs, force: bool) -> None:
     nvcc = os.path.join(cuda, "bin", "nvcc")
     lib64 = os.path.join(cuda, "lib64")
     cmd = [nvcc, *ARCH, "-shared", "-cudart", "static", "-o", out, *objs, "-L" + lib64,
-           "-lcublas", "-Xlinker", "-rpath", "-Xlinker", lib64, "-lpthread"]
+           "-Xlinker", "-rpath", "-Xlinker", lib64, "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

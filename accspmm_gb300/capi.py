@@ -150,6 +150,7 @@ _SIGS = {
     "accspmm_batch_destroy": ([vp], None),
     "accspmm_spmm_bias_act": ([C.POINTER(METCF), vp, vp, u32, i32, vp, i32, vp], C.c_int),
     "accspmm_gcn_layer": ([C.POINTER(METCF), vp, u32, vp, u32, vp, i32, vp, i32, vp], C.c_int),
+    "accspmm_dense_matmul": ([vp, u32, u32, vp, u32, vp, i32, vp], C.c_int),
     "accspmm_spmm_chain": ([C.POINTER(METCF), vp, vp, u32, u32, i32, vp], C.c_int),
     "accspmm_gather_floor": ([C.POINTER(METCF), vp, u32, u32, i32, f32p, vp], C.c_int),
     "accspmm_spmm_host": ([C.POINTER(METCF), C.POINTER(ADPBME), vp, vp, u32, i32, vp], C.c_int),

@@ -375,6 +375,12 @@ int accspmm_gcn_layer(const accspmm_metcf_t* adj, const float* H, uint32_t k_in,
     return gcn_layer_impl(adj, H, k_in, W, k_out, bias, activation, out, precision, stream);
 }
 
+int accspmm_dense_matmul(const float* H, uint32_t n, uint32_t k_in, const float* W, uint32_t k_out,
+                         float* XW, int32_t precision, void* stream) {
+    clear_error();
+    return dense_gemm_impl(H, n, k_in, W, k_out, XW, precision, static_cast<cudaStream_t>(stream));
+}
+
 int accspmm_spmm_chain(const accspmm_metcf_t* metcf, const float* B, float* C, uint32_t K,
                        uint32_t hops, int32_t precision, void* stream) {
     clear_error();
@@ -432,7 +438,15 @@ void accspmm_autotune_clear(void) { autotune_clear(); }
 
 int accspmm_device_status(void* stream) {
     clear_error();
-    return device_status_impl(stream);
+    // the SpMM kernels' word (the stream is synchronised first), then the
+    // dense GEMM's; both are cleared by reading them
+    const int r = device_status_impl(stream);
+    unsigned int g = 0;
+    const int rg = dense_gemm_status_take(&g);
+    if (r) return r;
+    if (rg) return rg;
+    if (g) ACC_FAIL(ACCSPMM_ERROR_TIMEOUT, "a bounded wait in the dense GEMM kernel expired");
+    return ACCSPMM_SUCCESS;
 }
 
 int accspmm_selftest_bounded_wait(uint32_t limit_ms, void* stream) {

@@ -1,0 +1,505 @@
+// dense_gemm.cu -- XW = H W for the graph-convolution layer, on the fifth-
+// generation tensor cores: tcgen05.mma kind::tf32 with the accumulator in
+// tensor memory, operands staged in shared memory by the tensor-map copy
+// engine (cp.async.bulk.tensor, 128-byte swizzle).  No counterpart in the
+// reference, which multiplies A by a constant B only (src/mma_tf32.cu:185-243);
+// this is the dense product of accspmm_gcn_layer and accspmm_dense_matmul.
+//
+// Shapes: H is n x k_in, W is k_in x k_out, both row-major fp32, n large
+// (graph rows) and k_in, k_out feature widths.  A CTA computes a 128-row by
+// NT-column tile of XW (NT = k_out rounded up to 16, at most 256 in TF32 and
+// 128 in 3xTF32; wider outputs take several column tiles), walking k_in in blocks of 32 through a
+// ring of shared-memory stages: per block one TMA copy of the 128 x 32 tile
+// of H and one of the NT x 32 tile of W^T (W transposed once per call into a
+// K-major pool buffer, so that both operands are K-major).  Every thread then
+// rounds its share of the H tile to TF32 in place (cvt.rna, the rounding of
+// the SpMM's operands) and, in 3xTF32, writes the low part x - hi beside it;
+// one thread issues the MMAs (K = 8 each, four per block; three products
+// per K step in 3xTF32: hi*hi, hi*lo, lo*hi) and commits them to the stage's
+// "empty" barrier, which lets the copy of block k + S reuse the stage.  In
+// TF32 the accumulator (128 lanes x NT fp32 columns of tensor memory) runs
+// over all of k_in and is read back at the end with tcgen05.ld, one TMEM lane
+// (one row of XW) per thread; in 3xTF32 every block's partial is read back as
+// soon as it is done and summed in FP32 registers (see the kernel).
+//
+// Every wait is bounded (2 s of %globaltimer); a wait that runs out raises
+// a bit in the status word that accspmm_device_status reports, the CTA waits
+// (bounded) for its copies in flight and its MMAs, stores nothing, frees its
+// tensor memory and returns.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "accspmm.h"
+#include "common.hpp"
+#include "device_util.cuh"
+#include "mbarrier.cuh"
+#include "spmm_common.cuh"
+#include "spmm_internal.hpp"
+
+namespace accspmm {
+
+namespace {
+
+__device__ unsigned int g_gemm_status = 0;
+
+constexpr int kBM = 128;       // rows of H per CTA: the MMA's M
+constexpr int kBK = 32;        // k per stage: one 128-byte swizzle row of fp32
+constexpr int kThreads = 128;  // four warps, one TMEM lane quarter each
+constexpr uint32_t kATileBytes = kBM * kBK * 4;  // 16 KB
+
+// Shared-memory matrix descriptor of a K-major operand tile written by a TMA
+// copy with 128-byte swizzle: rows of 128 bytes (32 fp32 along k), 8-row
+// groups 1024 bytes apart (stride byte offset), tile base 1024-byte aligned.
+// Fields: start address >> 4 (bits 0-13), leading byte offset >> 4 (16-29;
+// not used by swizzled K-major layouts whose MMA k fits in one row), stride
+// byte offset >> 4 (32-45), descriptor version 1 (46-47), base offset 0
+// (49-51), swizzle mode 2 = 128 B (61-63).
+__device__ __forceinline__ uint64_t kmajor_sw128_desc(uint32_t saddr) {
+    return uint64_t((saddr & 0x3FFFFu) >> 4) | (uint64_t(1) << 16) | (uint64_t(1024 >> 4) << 32) |
+           (uint64_t(1) << 46) | (uint64_t(2) << 61);
+}
+
+// Instruction descriptor of tcgen05.mma kind::tf32: D fp32 (bits 4-5 = 1),
+// A and B TF32 (bits 7-9, 10-12 = 2), both K-major (bits 15, 16 = 0),
+// N >> 3 (bits 17-22), M >> 4 (bits 24-28).
+__host__ __device__ constexpr uint32_t idesc_tf32(uint32_t m, uint32_t n) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* tm, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_tf32(uint32_t d_tmem, uint64_t da, uint64_t db, uint32_t idesc,
+                                          uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(da), "l"(db), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// The barrier gets one arrival once every MMA this thread issued so far is done.
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 16 consecutive fp32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+        "%13, %14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct GemmParams {
+    float* xw;        // n x k_out, row-major
+    uint32_t n, k_out;
+    uint32_t kblocks;  // ceil(k_in / 32)
+    uint32_t nt;       // output columns per CTA (multiple of 16; <= 256, 3xTF32 <= 128)
+    uint32_t stages;
+    uint32_t tmem_cols;  // power of two >= max(32, nt)
+    uint32_t stage_bytes;
+};
+
+// Shared memory of one stage: [A hi 16 KB][A lo 16 KB, 3xTF32][B hi nt*128][B lo nt*128, 3xTF32],
+// every part 1024-byte aligned (nt is a multiple of 16, so nt * 128 is a multiple of 2048).
+template <bool SPLIT>
+__host__ __device__ constexpr uint32_t stage_bytes_for(uint32_t nt) {
+    return (SPLIT ? 2u : 1u) * (kATileBytes + nt * 128u);
+}
+
+template <bool SPLIT>
+__global__ void __launch_bounds__(kThreads, 1)
+    dense_gemm_kernel(const __grid_constant__ CUtensorMap tm_h, const __grid_constant__ CUtensorMap tm_w,
+                      const __grid_constant__ CUtensorMap tm_wlo, const GemmParams p) {
+    extern __shared__ uint8_t dyn_smem[];
+    __shared__ __align__(8) uint64_t bars[2 * 8 + 3];  // full[8], empty[8], done, block done[2] (3xTF32)
+    __shared__ uint32_t s_tmem;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t S = p.stages;
+    const uint32_t base = (smem_addr(dyn_smem) + 1023u) & ~1023u;
+    uint8_t* gbase = dyn_smem + (base - smem_addr(dyn_smem));
+    auto full = [&](uint32_t s) { return smem_addr(&bars[s]); };
+    auto empty = [&](uint32_t s) { return smem_addr(&bars[8 + s]); };
+    const uint32_t done = smem_addr(&bars[16]);
+    auto bdone = [&](uint32_t r) { return smem_addr(&bars[17 + r]); };
+    const uint32_t a_hi = 0, a_lo = kATileBytes, b_hi = (SPLIT ? 2u : 1u) * kATileBytes,
+                   b_lo = b_hi + p.nt * 128u;
+    const uint32_t b_bytes = p.nt * 128u;
+    const uint32_t tx_bytes = kATileBytes + (SPLIT ? 2u : 1u) * b_bytes;
+
+    if (tid == 0) {
+        for (uint32_t s = 0; s < S; ++s) {
+            mbar_init(full(s), 1);
+            mbar_init(empty(s), 1);
+        }
+        mbar_init(done, 1);
+        mbar_init(bdone(0), 1);
+        mbar_init(bdone(1), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&s_tmem)),
+                     "r"(p.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = s_tmem;
+    const int m0 = int(blockIdx.x) * kBM;
+    const int n0 = int(blockIdx.y * p.nt);
+    const uint32_t idesc = idesc_tf32(kBM, p.nt);
+
+    uint32_t issued = 0;  // k-blocks whose copies were issued (thread 0)
+    bool stop = false;    // thread 0: a stage never came free, issue nothing more
+    auto issue = [&](uint32_t k) {
+        const uint32_t st = base + (k % S) * p.stage_bytes;
+        mbar_expect_tx(full(k % S), tx_bytes);
+        tma_load_2d(st + a_hi, &tm_h, int(k * kBK), m0, full(k % S));
+        tma_load_2d(st + b_hi, &tm_w, int(k * kBK), n0, full(k % S));
+        if (SPLIT) tma_load_2d(st + b_lo, &tm_wlo, int(k * kBK), n0, full(k % S));
+    };
+    if (tid == 0) {
+        for (; issued < S && issued < p.kblocks; ++issued) issue(issued);
+    }
+
+    // 3xTF32: each k-block's products go to their own tensor-memory region
+    // (block k to region k % 2: hi*hi in its first 128 columns, the two
+    // correction products in the next 128), and the block's partial is added
+    // to FP32 registers with round-to-nearest as soon as it is done; the
+    // tensor core accumulates only the four K = 8 steps of one block.  (One
+    // accumulator over all of k_in truncates at every step: 1.8e-6 relative
+    // error at k_in = 256, against about 2e-7 this way.)
+    float acc[SPLIT ? 128 : 1];
+#pragma unroll
+    for (int i = 0; i < (SPLIT ? 128 : 1); ++i) acc[i] = 0.f;
+    const uint32_t t_lane = (warp * 32u) << 16;
+    auto drain = [&](uint32_t b) -> bool {
+        const bool fin_b = __syncthreads_and(mbar_wait(bdone(b & 1u), (b >> 1) & 1u));
+        if (!fin_b) return false;
+        tc_fence_after();
+        const uint32_t t_main = tmem + t_lane + (b & 1u) * 256u;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            if (uint32_t(c) * 16u < p.nt) {
+                float v[16], w[16];
+                tmem_ld16(t_main + c * 16, v);
+                tmem_ld16(t_main + 128 + c * 16, w);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) acc[c * 16 + i] += v[i] + w[i];
+            }
+        }
+        tc_fence_before();
+        return true;
+    };
+
+    bool ok = true;
+    uint32_t k = 0;
+    for (; k < p.kblocks; ++k) {
+        const uint32_t s = k % S, ph = (k / S) & 1u;
+        const bool landed = mbar_wait(full(s), ph);
+        if (!__syncthreads_and(landed)) {
+            ok = false;
+            break;
+        }
+        // round the H tile to TF32 in place (and keep the low part in 3xTF32)
+        uint8_t* st = gbase + s * p.stage_bytes;
+        float4* ah = reinterpret_cast<float4*>(st + a_hi);
+        float4* al = reinterpret_cast<float4*>(st + a_lo);
+#pragma unroll
+        for (int i = 0; i < int(kATileBytes / 16 / kThreads); ++i) {
+            const uint32_t idx = tid + uint32_t(i) * kThreads;
+            float4 x = ah[idx];
+            float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
+            ah[idx] = h;
+            if (SPLIT)
+                al[idx] = make_float4(tf32_hi(x.x - h.x), tf32_hi(x.y - h.y), tf32_hi(x.z - h.z),
+                                      tf32_hi(x.w - h.w));
+        }
+        // generic-proxy writes made visible to the tensor core's (async) reads
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t sa = base + s * p.stage_bytes;
+#pragma unroll
+            for (uint32_t j = 0; j < kBK / 8; ++j) {
+                const uint64_t dah = kmajor_sw128_desc(sa + a_hi + j * 32);
+                const uint64_t dbh = kmajor_sw128_desc(sa + b_hi + j * 32);
+                if (SPLIT) {
+                    const uint32_t t_main = tmem + (k & 1u) * 256u;
+                    const uint64_t dal = kmajor_sw128_desc(sa + a_lo + j * 32);
+                    const uint64_t dbl = kmajor_sw128_desc(sa + b_lo + j * 32);
+                    umma_tf32(t_main, dah, dbh, idesc, j > 0 ? 1u : 0u);
+                    umma_tf32(t_main + 128, dal, dbh, idesc, j > 0 ? 1u : 0u);
+                    umma_tf32(t_main + 128, dah, dbl, idesc, 1u);
+                } else {
+                    umma_tf32(tmem, dah, dbh, idesc, (k > 0 || j > 0) ? 1u : 0u);
+                }
+            }
+            umma_commit(empty(s));
+            if (SPLIT) umma_commit(bdone(k & 1u));
+            if (!stop && issued < p.kblocks) {
+                // the stage is reused once the MMAs that read it are done
+                if (mbar_wait(empty(s), ph)) {
+                    issue(issued);
+                    ++issued;
+                } else {
+                    atomicOr(&g_gemm_status, 1u);
+                    stop = true;  // the wait for the block never issued fails for every thread
+                }
+            }
+        }
+        // 3xTF32: the previous block's partial into the registers (its region
+        // is written again by block k + 1, after the next barrier)
+        if (SPLIT && k > 0 && !drain(k - 1)) {
+            ok = false;
+            break;
+        }
+    }
+    if (SPLIT && ok && p.kblocks > 0 && !drain(p.kblocks - 1)) ok = false;
+    if (tid == 0) {
+        if (!ok) {
+            atomicOr(&g_gemm_status, 1u);
+            // copies still in flight must land before the CTA exits
+            for (uint32_t j = k; j < issued; ++j) mbar_wait(full(j % S), (j / S) & 1u);
+        }
+        umma_commit(done);
+    }
+    const bool fin = __syncthreads_and(mbar_wait(done, 0));  // uniform: tcgen05.ld is warp-wide
+    if (!fin && tid == 0) atomicOr(&g_gemm_status, 1u);
+    tc_fence_after();
+    if (SPLIT && ok && fin) {
+        const int row = m0 + int(warp * 32 + lane);
+        if (row < int(p.n)) {
+            float* dst = p.xw + size_t(row) * p.k_out + n0;
+#pragma unroll
+            for (int q = 0; q < 32; ++q)
+                if (uint32_t(q) * 4u < p.nt && uint32_t(n0) + 4u * q < p.k_out)
+                    reinterpret_cast<float4*>(dst)[q] =
+                        make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
+        }
+    }
+    if (!SPLIT && ok && fin) {
+        const int row = m0 + int(warp * 32 + lane);
+        const uint32_t t_row = tmem + ((warp * 32u) << 16);
+        for (uint32_t c = 0; c < p.nt; c += 16) {
+            float v[16];
+            tmem_ld16(t_row + c, v);
+            if (row < int(p.n)) {
+                float* dst = p.xw + size_t(row) * p.k_out + n0 + c;
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (uint32_t(n0) + c + 4 * q < p.k_out)
+                        reinterpret_cast<float4*>(dst)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(p.tmem_cols)
+                     : "memory");
+    }
+}
+
+// W (k_in x k_out, row-major) to K-major W^T (k_out x kp, kp = k_in rounded
+// up to 4, zeros past k_in); in 3xTF32 also the split hi = rna(w), lo =
+// rna(w - hi) of every value.
+__global__ void transpose_w_kernel(const float* __restrict__ w, uint32_t k_in, uint32_t k_out, uint32_t kp,
+                                   float* __restrict__ wt, float* __restrict__ wt_lo) {
+    const size_t total = size_t(k_out) * kp;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+        const uint32_t j = uint32_t(i / kp), kk = uint32_t(i % kp);
+        const float x = kk < k_in ? w[size_t(kk) * k_out + j] : 0.f;
+        if (wt_lo) {
+            const float h = tf32_hi(x);
+            wt[i] = h;
+            wt_lo[i] = tf32_hi(x - h);
+        } else {
+            wt[i] = tf32_hi(x);
+        }
+    }
+}
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+// (the library links the runtime statically and not libcuda).
+int encode_tiled(EncodeTiledFn* out) {
+    static std::mutex mu;
+    static EncodeTiledFn fn = nullptr;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!fn) {
+        void* ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000,
+                                                               cudaEnableDefault, &q);
+        if (e != cudaSuccess || !ptr || q != cudaDriverEntryPointSuccess)
+            ACC_FAIL(ACCSPMM_ERROR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+        fn = reinterpret_cast<EncodeTiledFn>(ptr);
+    }
+    *out = fn;
+    return ACCSPMM_SUCCESS;
+}
+
+// Tensor map of a row-major fp32 matrix of `rows` x `cols` (cols % 4 == 0,
+// 16-byte aligned base) read in boxes of 32 columns x box_rows rows with
+// 128-byte swizzle; reads past either edge return zeros.
+int fp32_kmajor_map(EncodeTiledFn enc, CUtensorMap* tm, const float* base, uint64_t rows, uint64_t cols,
+                    uint32_t box_rows) {
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {cols * 4};
+    const cuuint32_t box[2] = {uint32_t(kBK), box_rows};
+    const cuuint32_t es[2] = {1, 1};
+    const CUresult cr = enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, es,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (cr != CUDA_SUCCESS) ACC_FAIL(ACCSPMM_ERROR_CUDA, "cuTensorMapEncodeTiled failed (%d)", int(cr));
+    return ACCSPMM_SUCCESS;
+}
+
+template <bool SPLIT>
+int launch_gemm(const CUtensorMap& th, const CUtensorMap& tw, const CUtensorMap& twl, GemmParams p,
+                cudaStream_t s) {
+    // stages: as many as fit in about 200 KB (at least two, at most eight and
+    // at most the number of k-blocks)
+    p.stage_bytes = stage_bytes_for<SPLIT>(p.nt);
+    uint32_t st = (200u * 1024u) / p.stage_bytes;
+    st = st < 2 ? 2 : (st > 8 ? 8 : st);
+    if (st > p.kblocks) st = p.kblocks;
+    p.stages = st;
+    size_t smem = size_t(st) * p.stage_bytes + 1024;
+    // at most 512 / tmem_cols CTAs per SM, so that every CTA's tensor-memory
+    // allocation is granted at once: pad the shared memory (228 KB per SM)
+    const size_t cmax = 512 / p.tmem_cols;
+    const size_t smem_min = (228u * 1024u) / (cmax + 1) + 1;
+    if (smem < smem_min) smem = smem_min;
+    // dynamic shared memory, leaving room for the kernel's static barriers
+    constexpr size_t kMaxDyn = 226 * 1024;
+    if (smem > kMaxDyn) ACC_FAIL(ACCSPMM_ERROR_UNSUPPORTED, "shared memory %zu too large", smem);
+    static unsigned attr_set = 0;  // one bit per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 32 && !(attr_set & (1u << dev))) {
+        ACC_CUDA(cudaFuncSetAttribute(dense_gemm_kernel<SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      int(kMaxDyn)));
+        attr_set |= 1u << dev;
+    }
+    const dim3 grid((p.n + kBM - 1) / kBM, (p.k_out + p.nt - 1) / p.nt);
+    dense_gemm_kernel<SPLIT><<<grid, kThreads, smem, s>>>(th, tw, twl, p);
+    ACC_LAUNCH_CHECK();
+    return ACCSPMM_SUCCESS;
+}
+
+}  // namespace
+
+int dense_gemm_status_take(unsigned int* v) {
+    ACC_CUDA(cudaMemcpyFromSymbol(v, g_gemm_status, sizeof *v));
+    if (*v) {
+        const unsigned int z = 0;
+        ACC_CUDA(cudaMemcpyToSymbol(g_gemm_status, &z, sizeof z));
+    }
+    return ACCSPMM_SUCCESS;
+}
+
+int dense_gemm_impl(const float* H, uint32_t n, uint32_t k_in, const float* W, uint32_t k_out, float* XW,
+                    int precision, cudaStream_t s) {
+    if (k_in == 0 || k_out == 0 || k_out % 4)
+        ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "k_in > 0 and k_out a positive multiple of 4 required");
+    if (precision != ACCSPMM_PREC_TF32 && precision != ACCSPMM_PREC_3XTF32)
+        ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "unknown precision %d", precision);
+    if (n == 0) return ACCSPMM_SUCCESS;  // nothing to read or write
+    if (!H || !W || !XW) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "H, W and XW must be device pointers");
+    if (reinterpret_cast<uintptr_t>(XW) & 15u) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "XW must be 16-byte aligned");
+    const bool split = precision == ACCSPMM_PREC_3XTF32;
+    cudaMemPool_t pool = nullptr;
+    int r = library_pool(&pool);
+    if (r) return r;
+    EncodeTiledFn enc = nullptr;
+    if ((r = encode_tiled(&enc))) return r;
+    const uint32_t kp = (k_in + 3) & ~3u;
+    // H as the tensor map needs it: 16-byte aligned rows of kp floats
+    const float* h = H;
+    float* hp = nullptr;
+    float* wt = nullptr;
+    auto give_back = [&]() {
+        if (hp) cudaFreeAsync(hp, s);
+        if (wt) cudaFreeAsync(wt, s);
+    };
+    if (kp != k_in || (reinterpret_cast<uintptr_t>(H) & 15u)) {
+        const size_t bytes = size_t(n) * kp * 4;
+        cudaError_t ce = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&hp), bytes, pool, s);
+        if (ce != cudaSuccess) ACC_FAIL(ACCSPMM_ERROR_ALLOC, "pool allocation failed: %s", cudaGetErrorString(ce));
+        ce = cudaMemsetAsync(hp, 0, bytes, s);
+        if (ce == cudaSuccess)
+            ce = cudaMemcpy2DAsync(hp, size_t(kp) * 4, H, size_t(k_in) * 4, size_t(k_in) * 4, n,
+                                   cudaMemcpyDeviceToDevice, s);
+        if (ce != cudaSuccess) {
+            give_back();
+            ACC_FAIL(ACCSPMM_ERROR_CUDA, "copy of H failed: %s", cudaGetErrorString(ce));
+        }
+        h = hp;
+    }
+    // W^T, K-major (and its low parts in 3xTF32), rounded to TF32
+    const size_t wn = size_t(k_out) * kp;
+    cudaError_t ce = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&wt), wn * 4 * (split ? 2 : 1), pool, s);
+    if (ce != cudaSuccess) {
+        give_back();
+        ACC_FAIL(ACCSPMM_ERROR_ALLOC, "pool allocation failed: %s", cudaGetErrorString(ce));
+    }
+    float* wt_lo = split ? wt + wn : nullptr;
+    {
+        const unsigned blocks = unsigned(std::min<size_t>((wn + 255) / 256, 4096));
+        transpose_w_kernel<<<blocks, 256, 0, s>>>(W, k_in, k_out, kp, wt, wt_lo);
+        const cudaError_t le = cudaGetLastError();
+        if (le != cudaSuccess) {
+            give_back();
+            ACC_FAIL(ACCSPMM_ERROR_CUDA, "transpose launch failed: %s", cudaGetErrorString(le));
+        }
+    }
+    GemmParams p{};
+    p.xw = XW;
+    p.n = n;
+    p.k_out = k_out;
+    p.kblocks = (kp + kBK - 1) / kBK;
+    // TF32: up to 256 output columns per CTA, one accumulator; 3xTF32: up to
+    // 128, four 128-column regions (two blocks in flight, main and correction
+    // products each)
+    p.nt = std::min<uint32_t>(split ? 128 : 256, (k_out + 15) & ~15u);
+    p.tmem_cols = 32;
+    while (p.tmem_cols < p.nt) p.tmem_cols <<= 1;
+    if (split) p.tmem_cols = 512;
+    CUtensorMap th, tw, twl;
+    r = fp32_kmajor_map(enc, &th, h, n, kp, kBM);
+    if (!r) r = fp32_kmajor_map(enc, &tw, wt, k_out, kp, p.nt);
+    if (!r) r = fp32_kmajor_map(enc, &twl, split ? wt_lo : wt, k_out, kp, p.nt);
+    if (!r) r = split ? launch_gemm<true>(th, tw, twl, p, s) : launch_gemm<false>(th, tw, twl, p, s);
+    give_back();
+    return r;
+}
+
+}  // namespace accspmm

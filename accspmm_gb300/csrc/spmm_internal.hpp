@@ -65,6 +65,12 @@ int spmm_bias_act_impl(const accspmm_metcf_t* m, const float* B, float* C, uint3
 int gcn_layer_impl(const accspmm_metcf_t* adj, const float* H, uint32_t k_in, const float* W,
                    uint32_t k_out, const float* bias, int act, float* out, int precision,
                    void* stream);
+// XW = H W (n x k_in times k_in x k_out, row-major fp32) on the tcgen05
+// tensor cores, TF32 or 3xTF32 (dense_gemm.cu).
+int dense_gemm_impl(const float* H, uint32_t n, uint32_t k_in, const float* W, uint32_t k_out, float* XW,
+                    int precision, cudaStream_t s);
+// Reads and clears the dense GEMM's status word (1: a bounded wait expired).
+int dense_gemm_status_take(unsigned int* v);
 int permute_rows_impl(const float* src, float* dst, const uint32_t* idx, uint32_t rows, uint32_t K,
                       int scatter, void* stream);
 int spmm_chain_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K, uint32_t hops,

@@ -195,7 +195,8 @@ def peaks():
 # the reason).
 KERNEL_SOURCES = ("accspmm_gb300/csrc/spmm.cu", "accspmm_gb300/csrc/spmm_direct.cuh",
                   "accspmm_gb300/csrc/spmm_common.cuh")
-TRAFFIC = {}
+TRAFFIC = {128: {"bytes": 8052258933, "src_sha": "98654848eac34155",
+                 "capture": "profiles/spmm_window_packed_kernel_powerlaw_local.md"}}
 
 
 def kernel_source_hash():

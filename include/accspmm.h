@@ -293,14 +293,27 @@ int accspmm_spmm_bias_act(const accspmm_metcf_t* metcf, const float* B, float* C
 
 /* One graph-convolution layer, out = act(A (H W) + bias): H is cols x k_in,
  * W is k_in x k_out (row-major, device), out is 8 num_windows x k_out.  H W
- * is computed by cuBLAS (TF32 tensor cores for ACCSPMM_PREC_TF32, FP32 for
- * ACCSPMM_PREC_3XTF32) into a buffer from the library's memory pool, then
+ * is computed by accspmm_dense_matmul (tcgen05 tensor cores, TF32 or 3xTF32
+ * as `precision` says) into a buffer from the library's memory pool, then
  * multiplied by A with the bias/activation epilogue of accspmm_spmm_bias_act.
  * k_out must be a multiple of 4.  No counterpart in the reference. */
 int accspmm_gcn_layer(const accspmm_metcf_t* adj, const float* H, uint32_t k_in,
                       const float* W, uint32_t k_out, const float* bias,
                       int32_t activation, float* out, int32_t precision,
                       void* stream);
+
+/* Dense product XW = H W on the device: H is n x k_in, W is k_in x k_out and
+ * XW is n x k_out, all row-major fp32 (XW 16-byte aligned, k_out a positive
+ * multiple of 4).  The dense half of accspmm_gcn_layer, run on the tcgen05
+ * tensor cores with the accumulator in tensor memory: TF32 (both operands
+ * rounded with cvt.rna, FP32 accumulation) or 3xTF32 (hi/lo splits, near-FP32
+ * accuracy).  Temporary buffers (W transposed; H repacked when k_in is not a
+ * multiple of 4 or H is not 16-byte aligned) come from the library's memory
+ * pool; n = 0 is a no-op.  Enqueued on `stream`; a bounded wait that expires inside the kernel
+ * is reported by accspmm_device_status.  No counterpart in the reference
+ * (its driver multiplies A by a constant B only, src/mma_tf32.cu:185-243). */
+int accspmm_dense_matmul(const float* H, uint32_t n, uint32_t k_in, const float* W,
+                         uint32_t k_out, float* XW, int32_t precision, void* stream);
 
 /* Multi-hop propagation C = A^hops B of a square matrix, all on the device:
  * hops launches of accspmm_spmm_tf32, each product feeding the next through
