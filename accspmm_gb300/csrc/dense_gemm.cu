@@ -6,21 +6,22 @@
 // this is the dense product of accspmm_gcn_layer and accspmm_dense_matmul.
 //
 // Shapes: H is n x k_in, W is k_in x k_out, both row-major fp32, n large
-// (graph rows) and k_in, k_out feature widths.  A CTA computes a 128-row by
-// NT-column tile of XW (NT = k_out rounded up to 16, at most 256 in TF32 and
-// 128 in 3xTF32; wider outputs take several column tiles), walking k_in in blocks of 32 through a
-// ring of shared-memory stages: per block one TMA copy of the 128 x 32 tile
-// of H and one of the NT x 32 tile of W^T (W transposed once per call into a
-// K-major pool buffer, so that both operands are K-major).  Every thread then
-// rounds its share of the H tile to TF32 in place (cvt.rna, the rounding of
-// the SpMM's operands) and, in 3xTF32, writes the low part x - hi beside it;
-// one thread issues the MMAs (K = 8 each, four per block; three products
-// per K step in 3xTF32: hi*hi, hi*lo, lo*hi) and commits them to the stage's
-// "empty" barrier, which lets the copy of block k + S reuse the stage.  In
-// TF32 the accumulator (128 lanes x NT fp32 columns of tensor memory) runs
-// over all of k_in and is read back at the end with tcgen05.ld, one TMEM lane
-// (one row of XW) per thread; in 3xTF32 every block's partial is read back as
-// soon as it is done and summed in FP32 registers (see the kernel).
+// (graph rows) and k_in, k_out feature widths.  Work is cut into 128-row by
+// NT-column tiles of XW (NT = k_out rounded up to 16, at most 256 in TF32 and
+// 128 in 3xTF32; wider outputs take several column tiles); k_in is walked in
+// blocks of 32 through a ring of shared-memory stages, each holding the
+// 128 x 32 block of H and the NT x 32 block of W^T (W transposed and rounded
+// to TF32 once per call into a K-major pool buffer, so that both operands are
+// K-major), copied by tensor-map loads.  The H block is rounded to TF32 in
+// place (cvt.rna, the rounding of the SpMM's operands) before the MMAs read
+// it; the MMAs are tcgen05.mma with K = 8, four per block.
+//
+// TF32 (dense_gemm_tf32_ws_kernel): persistent and warp-specialised -- copies,
+// rounding, MMAs into two alternating TMEM accumulators, and stores through
+// shared memory and tensor-map stores all overlap (described at the kernel).
+// 3xTF32 (dense_gemm_3xtf32_kernel): one tile per CTA; H and W are split into
+// hi + lo TF32 parts, three products per K step (hi*hi, hi*lo, lo*hi), and
+// every block's partial is summed in FP32 registers (described at the kernel).
 //
 // Every wait is bounded (2 s of %globaltimer); a wait that runs out raises
 // a bit in the status word that accspmm_device_status reports, the CTA waits
@@ -119,16 +120,14 @@ struct GemmParams {
     uint32_t stage_bytes;
 };
 
-// Shared memory of one stage: [A hi 16 KB][A lo 16 KB, 3xTF32][B hi nt*128][B lo nt*128, 3xTF32],
+// Shared memory of one 3xTF32 stage: [A hi 16 KB][A lo 16 KB][B hi nt*128][B lo nt*128],
 // every part 1024-byte aligned (nt is a multiple of 16, so nt * 128 is a multiple of 2048).
-template <bool SPLIT>
-__host__ __device__ constexpr uint32_t stage_bytes_for(uint32_t nt) {
-    return (SPLIT ? 2u : 1u) * (kATileBytes + nt * 128u);
-}
+__host__ __device__ constexpr uint32_t split_stage_bytes(uint32_t nt) { return 2u * (kATileBytes + nt * 128u); }
 
-template <bool SPLIT>
+// 3xTF32: one 128 x NT tile per CTA, every thread rounding and splitting
+// the H blocks, one thread issuing the MMAs (see the file's header).
 __global__ void __launch_bounds__(kThreads, 1)
-    dense_gemm_kernel(const __grid_constant__ CUtensorMap tm_h, const __grid_constant__ CUtensorMap tm_w,
+    dense_gemm_3xtf32_kernel(const __grid_constant__ CUtensorMap tm_h, const __grid_constant__ CUtensorMap tm_w,
                       const __grid_constant__ CUtensorMap tm_wlo, const GemmParams p) {
     extern __shared__ uint8_t dyn_smem[];
     __shared__ __align__(8) uint64_t bars[2 * 8 + 3];  // full[8], empty[8], done, block done[2] (3xTF32)
@@ -141,10 +140,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     auto empty = [&](uint32_t s) { return smem_addr(&bars[8 + s]); };
     const uint32_t done = smem_addr(&bars[16]);
     auto bdone = [&](uint32_t r) { return smem_addr(&bars[17 + r]); };
-    const uint32_t a_hi = 0, a_lo = kATileBytes, b_hi = (SPLIT ? 2u : 1u) * kATileBytes,
-                   b_lo = b_hi + p.nt * 128u;
-    const uint32_t b_bytes = p.nt * 128u;
-    const uint32_t tx_bytes = kATileBytes + (SPLIT ? 2u : 1u) * b_bytes;
+    const uint32_t a_hi = 0, a_lo = kATileBytes, b_hi = 2u * kATileBytes, b_lo = b_hi + p.nt * 128u;
+    const uint32_t tx_bytes = kATileBytes + 2u * p.nt * 128u;
 
     if (tid == 0) {
         for (uint32_t s = 0; s < S; ++s) {
@@ -177,22 +174,22 @@ __global__ void __launch_bounds__(kThreads, 1)
         mbar_expect_tx(full(k % S), tx_bytes);
         tma_load_2d(st + a_hi, &tm_h, int(k * kBK), m0, full(k % S));
         tma_load_2d(st + b_hi, &tm_w, int(k * kBK), n0, full(k % S));
-        if (SPLIT) tma_load_2d(st + b_lo, &tm_wlo, int(k * kBK), n0, full(k % S));
+        tma_load_2d(st + b_lo, &tm_wlo, int(k * kBK), n0, full(k % S));
     };
     if (tid == 0) {
         for (; issued < S && issued < p.kblocks; ++issued) issue(issued);
     }
 
-    // 3xTF32: each k-block's products go to their own tensor-memory region
+    // Each k-block's products go to their own tensor-memory region
     // (block k to region k % 2: hi*hi in its first 128 columns, the two
     // correction products in the next 128), and the block's partial is added
     // to FP32 registers with round-to-nearest as soon as it is done; the
     // tensor core accumulates only the four K = 8 steps of one block.  (One
     // accumulator over all of k_in truncates at every step: 1.8e-6 relative
     // error at k_in = 256, against about 2e-7 this way.)
-    float acc[SPLIT ? 128 : 1];
+    float acc[128];
 #pragma unroll
-    for (int i = 0; i < (SPLIT ? 128 : 1); ++i) acc[i] = 0.f;
+    for (int i = 0; i < 128; ++i) acc[i] = 0.f;
     const uint32_t t_lane = (warp * 32u) << 16;
     auto drain = [&](uint32_t b) -> bool {
         const bool fin_b = __syncthreads_and(mbar_wait(bdone(b & 1u), (b >> 1) & 1u));
@@ -222,7 +219,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             ok = false;
             break;
         }
-        // round the H tile to TF32 in place (and keep the low part in 3xTF32)
+        // round the H tile to TF32 in place and keep the low part beside it
         uint8_t* st = gbase + s * p.stage_bytes;
         float4* ah = reinterpret_cast<float4*>(st + a_hi);
         float4* al = reinterpret_cast<float4*>(st + a_lo);
@@ -232,9 +229,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             float4 x = ah[idx];
             float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
             ah[idx] = h;
-            if (SPLIT)
-                al[idx] = make_float4(tf32_hi(x.x - h.x), tf32_hi(x.y - h.y), tf32_hi(x.z - h.z),
-                                      tf32_hi(x.w - h.w));
+            al[idx] = make_float4(tf32_hi(x.x - h.x), tf32_hi(x.y - h.y), tf32_hi(x.z - h.z),
+                                  tf32_hi(x.w - h.w));
         }
         // generic-proxy writes made visible to the tensor core's (async) reads
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -246,19 +242,15 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (uint32_t j = 0; j < kBK / 8; ++j) {
                 const uint64_t dah = kmajor_sw128_desc(sa + a_hi + j * 32);
                 const uint64_t dbh = kmajor_sw128_desc(sa + b_hi + j * 32);
-                if (SPLIT) {
-                    const uint32_t t_main = tmem + (k & 1u) * 256u;
-                    const uint64_t dal = kmajor_sw128_desc(sa + a_lo + j * 32);
-                    const uint64_t dbl = kmajor_sw128_desc(sa + b_lo + j * 32);
-                    umma_tf32(t_main, dah, dbh, idesc, j > 0 ? 1u : 0u);
-                    umma_tf32(t_main + 128, dal, dbh, idesc, j > 0 ? 1u : 0u);
-                    umma_tf32(t_main + 128, dah, dbl, idesc, 1u);
-                } else {
-                    umma_tf32(tmem, dah, dbh, idesc, (k > 0 || j > 0) ? 1u : 0u);
-                }
+                const uint32_t t_main = tmem + (k & 1u) * 256u;
+                const uint64_t dal = kmajor_sw128_desc(sa + a_lo + j * 32);
+                const uint64_t dbl = kmajor_sw128_desc(sa + b_lo + j * 32);
+                umma_tf32(t_main, dah, dbh, idesc, j > 0 ? 1u : 0u);
+                umma_tf32(t_main + 128, dal, dbh, idesc, j > 0 ? 1u : 0u);
+                umma_tf32(t_main + 128, dah, dbl, idesc, 1u);
             }
             umma_commit(empty(s));
-            if (SPLIT) umma_commit(bdone(k & 1u));
+            umma_commit(bdone(k & 1u));
             if (!stop && issued < p.kblocks) {
                 // the stage is reused once the MMAs that read it are done
                 if (mbar_wait(empty(s), ph)) {
@@ -270,14 +262,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
             }
         }
-        // 3xTF32: the previous block's partial into the registers (its region
-        // is written again by block k + 1, after the next barrier)
-        if (SPLIT && k > 0 && !drain(k - 1)) {
+        // the previous block's partial into the registers (its region is
+        // written again by block k + 1, after the next barrier)
+        if (k > 0 && !drain(k - 1)) {
             ok = false;
             break;
         }
     }
-    if (SPLIT && ok && p.kblocks > 0 && !drain(p.kblocks - 1)) ok = false;
+    if (ok && p.kblocks > 0 && !drain(p.kblocks - 1)) ok = false;
     if (tid == 0) {
         if (!ok) {
             atomicOr(&g_gemm_status, 1u);
@@ -289,7 +281,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const bool fin = __syncthreads_and(mbar_wait(done, 0));  // uniform: tcgen05.ld is warp-wide
     if (!fin && tid == 0) atomicOr(&g_gemm_status, 1u);
     tc_fence_after();
-    if (SPLIT && ok && fin) {
+    if (ok && fin) {
         const int row = m0 + int(warp * 32 + lane);
         if (row < int(p.n)) {
             float* dst = p.xw + size_t(row) * p.k_out + n0;
@@ -300,24 +292,260 @@ __global__ void __launch_bounds__(kThreads, 1)
                         make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
         }
     }
-    if (!SPLIT && ok && fin) {
-        const int row = m0 + int(warp * 32 + lane);
-        const uint32_t t_row = tmem + ((warp * 32u) << 16);
-        for (uint32_t c = 0; c < p.nt; c += 16) {
-            float v[16];
-            tmem_ld16(t_row + c, v);
-            if (row < int(p.n)) {
-                float* dst = p.xw + size_t(row) * p.k_out + n0 + c;
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    if (uint32_t(n0) + c + 4 * q < p.k_out)
-                        reinterpret_cast<float4*>(dst)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-            }
-        }
-    }
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(p.tmem_cols)
+                     : "memory");
+    }
+}
+
+// ---------------------------------------------------------------------------
+// TF32: a persistent, warp-specialised kernel.  Each CTA walks work items
+// (128-row x NT-column tiles of XW, column tile fastest) with five roles:
+//   warp 0, one lane   -- copies: the H and W^T blocks of every item into a
+//                         ring of S stages (tensor-map loads, "full" barriers);
+//   warps 2-5          -- round the H block of each landed stage to TF32 in
+//                         place (cvt.rna) and mark it ready ("conv");
+//   warp 1, one lane   -- MMAs: four K = 8 tcgen05.mma per block into one of
+//                         two tensor-memory accumulators (items alternate),
+//                         committing each stage back to the copier ("empty")
+//                         and each finished accumulator to the store warps
+//                         ("tfull");
+//   warps 6-9          -- store: each reads its 32 TMEM lanes (rows) of the
+//                         finished accumulator 32 columns at a time, writes
+//                         them to a swizzled 4 KB staging buffer and stores
+//                         it with a tensor-map store, then frees the
+//                         accumulator ("tempty").
+// So the copies of the next blocks, the rounding, the MMAs of item i + 1 and
+// the stores of item i all run at once.  Every wait is bounded: a wait that
+// runs out sets an abort flag that ends every role's loop, and raises the
+// status bit; each role then waits (bounded) for its own asynchronous work
+// and the CTA frees its tensor memory.
+
+constexpr int kWsThreads = 320;       // ten warps
+constexpr uint32_t kStageOut = 4096;  // one store warp's staging buffer: 32 rows x 32 fp32
+
+struct WsParams {
+    uint32_t n, k_out;
+    uint32_t kblocks;    // ceil(kp / 32)
+    uint32_t nt;         // output columns per item (multiple of 16, <= 256)
+    uint32_t n_tiles;    // column tiles: ceil(k_out / nt)
+    uint32_t items;      // ceil(n / 128) * n_tiles
+    uint32_t stages;
+    uint32_t stage_bytes;
+    uint32_t acc_stride;  // TMEM columns between the two accumulators (power of two >= max(32, nt))
+    uint32_t tmem_cols;   // 2 * acc_stride
+};
+
+__device__ __forceinline__ bool wait_or_abort(uint32_t bar, uint32_t parity, volatile int* abort) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (*abort) return false;
+        if (global_ns() - t0 > kWaitLimitNs) {
+            *abort = 1;
+            atomicOr(&g_gemm_status, 1u);
+            return false;
+        }
+    }
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(bar) : "memory");
+}
+
+// 32 consecutive fp32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* tm, int x, int y, uint32_t src) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                     reinterpret_cast<uint64_t>(tm)),
+                 "r"(x), "r"(y), "r"(src)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kWsThreads, 1)
+    dense_gemm_tf32_ws_kernel(const __grid_constant__ CUtensorMap tm_h, const __grid_constant__ CUtensorMap tm_w,
+                              const __grid_constant__ CUtensorMap tm_out, const WsParams p) {
+    extern __shared__ uint8_t dyn_smem[];
+    // full[8], conv[8], empty[8], tfull[2], tempty[2], done
+    __shared__ __align__(8) uint64_t bars[3 * 8 + 5];
+    __shared__ uint32_t s_tmem;
+    __shared__ volatile int s_abort;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t S = p.stages;
+    const uint32_t base = (smem_addr(dyn_smem) + 1023u) & ~1023u;
+    uint8_t* gbase = dyn_smem + (base - smem_addr(dyn_smem));
+    const uint32_t out_base = base + S * p.stage_bytes;  // 4 store warps x 2 buffers x 4 KB
+    auto full = [&](uint32_t s) { return smem_addr(&bars[s]); };
+    auto conv = [&](uint32_t s) { return smem_addr(&bars[8 + s]); };
+    auto empty = [&](uint32_t s) { return smem_addr(&bars[16 + s]); };
+    auto tfull = [&](uint32_t b) { return smem_addr(&bars[24 + b]); };
+    auto tempty = [&](uint32_t b) { return smem_addr(&bars[26 + b]); };
+    const uint32_t done = smem_addr(&bars[28]);
+    const uint32_t b_off = kATileBytes;
+    const uint32_t tx_bytes = kATileBytes + p.nt * 128u;
+
+    if (tid == 0) {
+        for (uint32_t s = 0; s < S; ++s) {
+            mbar_init(full(s), 1);
+            mbar_init(conv(s), 4);
+            mbar_init(empty(s), 1);
+        }
+        for (uint32_t b = 0; b < 2; ++b) {
+            mbar_init(tfull(b), 1);
+            mbar_init(tempty(b), 4);
+        }
+        mbar_init(done, 1);
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&s_tmem)),
+                     "r"(p.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = s_tmem;
+
+    if (warp == 0) {
+        // copier
+        if (lane == 0) {
+            uint32_t it = 0;
+            bool go = true;
+            for (uint32_t item = blockIdx.x; go && item < p.items; item += gridDim.x) {
+                const int m0 = int(item / p.n_tiles) * kBM, n0 = int((item % p.n_tiles) * p.nt);
+                for (uint32_t kb = 0; kb < p.kblocks; ++kb, ++it) {
+                    const uint32_t s = it % S, use = it / S;
+                    if (use > 0 && !wait_or_abort(empty(s), (use - 1) & 1u, &s_abort)) {
+                        go = false;
+                        break;
+                    }
+                    const uint32_t st = base + s * p.stage_bytes;
+                    mbar_expect_tx(full(s), tx_bytes);
+                    tma_load_2d(st, &tm_h, int(kb * kBK), m0, full(s));
+                    tma_load_2d(st + b_off, &tm_w, int(kb * kBK), n0, full(s));
+                }
+            }
+            // the last S copies may still be in flight when the loop ended early
+            const uint32_t first = it > S ? it - S : 0;
+            for (uint32_t i = first; i < it; ++i) mbar_wait(full(i % S), (i / S) & 1u);
+        }
+    } else if (warp == 1) {
+        // MMA issuer
+        if (lane == 0) {
+            const uint32_t idesc = idesc_tf32(kBM, p.nt);
+            uint32_t it = 0, t = 0;
+            bool go = true;
+            for (uint32_t item = blockIdx.x; go && item < p.items; item += gridDim.x, ++t) {
+                const uint32_t b = t & 1u, use_b = t >> 1;
+                if (use_b > 0 && !wait_or_abort(tempty(b), (use_b - 1) & 1u, &s_abort)) break;
+                tc_fence_after();
+                const uint32_t d = tmem + b * p.acc_stride;
+                for (uint32_t kb = 0; kb < p.kblocks; ++kb, ++it) {
+                    const uint32_t s = it % S;
+                    if (!wait_or_abort(conv(s), (it / S) & 1u, &s_abort)) {
+                        go = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t sa = base + s * p.stage_bytes;
+#pragma unroll
+                    for (uint32_t j = 0; j < kBK / 8; ++j)
+                        umma_tf32(d, kmajor_sw128_desc(sa + j * 32), kmajor_sw128_desc(sa + b_off + j * 32), idesc,
+                                  (kb > 0 || j > 0) ? 1u : 0u);
+                    umma_commit(empty(s));
+                }
+                if (go) umma_commit(tfull(b));
+            }
+            // no MMA may still run when the tensor memory is freed
+            umma_commit(done);
+            mbar_wait(done, 0);
+        }
+    } else if (warp < 6) {
+        // rounding: 128 threads, 8 float4 of each 16 KB H block
+        const uint32_t ct = tid - 64;
+        uint32_t it = 0;
+        bool go = true;
+        for (uint32_t item = blockIdx.x; go && item < p.items; item += gridDim.x) {
+            for (uint32_t kb = 0; kb < p.kblocks; ++kb, ++it) {
+                const uint32_t s = it % S;
+                const bool landed = __all_sync(0xffffffffu, wait_or_abort(full(s), (it / S) & 1u, &s_abort));
+                if (!landed) {
+                    go = false;
+                    break;
+                }
+                float4* ah = reinterpret_cast<float4*>(gbase + s * p.stage_bytes);
+#pragma unroll
+                for (int i = 0; i < int(kATileBytes / 16 / 128); ++i) {
+                    const uint32_t idx = ct + uint32_t(i) * 128u;
+                    const float4 x = ah[idx];
+                    ah[idx] = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(conv(s));
+            }
+        }
+    } else {
+        // stores: warp w reads TMEM lanes 32 (w % 4) .. +31, i.e. rows m0 + 32 (w % 4) + lane
+        const uint32_t q = warp & 3u;
+        const uint32_t obuf = out_base + (warp - 6) * 2 * kStageOut;
+        uint8_t* gobuf = gbase + (obuf - base);
+        uint32_t t = 0, nst = 0;
+        for (uint32_t item = blockIdx.x; item < p.items; item += gridDim.x, ++t) {
+            const uint32_t b = t & 1u;
+            const bool ready = __all_sync(0xffffffffu, wait_or_abort(tfull(b), (t >> 1) & 1u, &s_abort));
+            if (!ready) break;
+            tc_fence_after();
+            const int m0 = int(item / p.n_tiles) * kBM, n0 = int((item % p.n_tiles) * p.nt);
+            const uint32_t t_row = tmem + b * p.acc_stride + ((q * 32u) << 16);
+            for (uint32_t c = 0; c * 32 < p.nt; ++c) {
+                // chunks wholly past the matrix's rows or columns store nothing
+                if (uint32_t(m0) + q * 32u >= p.n || uint32_t(n0) + c * 32u >= p.k_out) continue;
+                ++nst;
+                uint32_t r[32];
+                tmem_ld32(t_row + c * 32, r);
+                // the store that used this buffer two chunks ago has read it
+                if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+                __syncwarp();
+                const uint32_t buf = (nst & 1u) * kStageOut;
+                uint8_t* row = gobuf + buf + lane * 128u;
+#pragma unroll
+                for (uint32_t j = 0; j < 8; ++j)
+                    *reinterpret_cast<uint4*>(row + ((j ^ (lane & 7u)) * 16u)) =
+                        make_uint4(r[4 * j], r[4 * j + 1], r[4 * j + 2], r[4 * j + 3]);
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) tma_store_2d(&tm_out, n0 + int(c * 32), m0 + int(q * 32), obuf + buf);
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(tempty(b));
+        }
+        if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        __syncwarp();
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(p.tmem_cols)
                      : "memory");
@@ -373,7 +601,7 @@ int fp32_kmajor_map(EncodeTiledFn enc, CUtensorMap* tm, const float* base, uint6
                     uint32_t box_rows) {
     const cuuint64_t dims[2] = {cols, rows};
     const cuuint64_t strides[1] = {cols * 4};
-    const cuuint32_t box[2] = {uint32_t(kBK), box_rows};
+    const cuuint32_t box[2] = {32u, box_rows};
     const cuuint32_t es[2] = {1, 1};
     const CUresult cr = enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, es,
                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -382,12 +610,11 @@ int fp32_kmajor_map(EncodeTiledFn enc, CUtensorMap* tm, const float* base, uint6
     return ACCSPMM_SUCCESS;
 }
 
-template <bool SPLIT>
-int launch_gemm(const CUtensorMap& th, const CUtensorMap& tw, const CUtensorMap& twl, GemmParams p,
-                cudaStream_t s) {
+int launch_gemm_3xtf32(const CUtensorMap& th, const CUtensorMap& tw, const CUtensorMap& twl, GemmParams p,
+                       cudaStream_t s) {
     // stages: as many as fit in about 200 KB (at least two, at most eight and
     // at most the number of k-blocks)
-    p.stage_bytes = stage_bytes_for<SPLIT>(p.nt);
+    p.stage_bytes = split_stage_bytes(p.nt);
     uint32_t st = (200u * 1024u) / p.stage_bytes;
     st = st < 2 ? 2 : (st > 8 ? 8 : st);
     if (st > p.kblocks) st = p.kblocks;
@@ -405,12 +632,37 @@ int launch_gemm(const CUtensorMap& th, const CUtensorMap& tw, const CUtensorMap&
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 32 && !(attr_set & (1u << dev))) {
-        ACC_CUDA(cudaFuncSetAttribute(dense_gemm_kernel<SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        ACC_CUDA(cudaFuncSetAttribute(dense_gemm_3xtf32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       int(kMaxDyn)));
         attr_set |= 1u << dev;
     }
     const dim3 grid((p.n + kBM - 1) / kBM, (p.k_out + p.nt - 1) / p.nt);
-    dense_gemm_kernel<SPLIT><<<grid, kThreads, smem, s>>>(th, tw, twl, p);
+    dense_gemm_3xtf32_kernel<<<grid, kThreads, smem, s>>>(th, tw, twl, p);
+    ACC_LAUNCH_CHECK();
+    return ACCSPMM_SUCCESS;
+}
+
+int launch_gemm_ws(const CUtensorMap& th, const CUtensorMap& tw, const CUtensorMap& tout, WsParams p,
+                   cudaStream_t s) {
+    constexpr size_t kMaxDyn = 226 * 1024;
+    const size_t fixed = 4 * 2 * kStageOut + 1024;  // store staging + alignment slack
+    p.stage_bytes = kATileBytes + p.nt * 128u;
+    uint32_t st = uint32_t((kMaxDyn - fixed) / p.stage_bytes);
+    p.stages = st > 8 ? 8 : st;
+    if (p.stages < 2) ACC_FAIL(ACCSPMM_ERROR_UNSUPPORTED, "shared memory too small for two stages");
+    size_t smem = size_t(p.stages) * p.stage_bytes + fixed;
+    // one CTA per SM: more than half of the SM's 228 KB
+    if (smem < 115 * 1024) smem = 115 * 1024;
+    static unsigned attr_set = 0;  // one bit per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 32 && !(attr_set & (1u << dev))) {
+        ACC_CUDA(cudaFuncSetAttribute(dense_gemm_tf32_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      int(kMaxDyn)));
+        attr_set |= 1u << dev;
+    }
+    const uint32_t grid = std::min<uint32_t>(p.items, uint32_t(sm_count()));
+    dense_gemm_tf32_ws_kernel<<<grid, kWsThreads, smem, s>>>(th, tw, tout, p);
     ACC_LAUNCH_CHECK();
     return ACCSPMM_SUCCESS;
 }
@@ -497,7 +749,24 @@ int dense_gemm_impl(const float* H, uint32_t n, uint32_t k_in, const float* W, u
     r = fp32_kmajor_map(enc, &th, h, n, kp, kBM);
     if (!r) r = fp32_kmajor_map(enc, &tw, wt, k_out, kp, p.nt);
     if (!r) r = fp32_kmajor_map(enc, &twl, split ? wt_lo : wt, k_out, kp, p.nt);
-    if (!r) r = split ? launch_gemm<true>(th, tw, twl, p, s) : launch_gemm<false>(th, tw, twl, p, s);
+    if (!r && split) r = launch_gemm_3xtf32(th, tw, twl, p, s);
+    if (!r && !split) {
+        // XW written by tensor-map stores of 32 x 32 boxes (rows past n and
+        // columns past k_out are not written)
+        CUtensorMap tout;
+        r = fp32_kmajor_map(enc, &tout, XW, n, k_out, 32);
+        WsParams w{};
+        w.n = n;
+        w.k_out = k_out;
+        w.kblocks = p.kblocks;
+        w.nt = p.nt;
+        w.n_tiles = (k_out + p.nt - 1) / p.nt;
+        w.items = ((n + kBM - 1) / kBM) * w.n_tiles;  // below 2^32: n < 2^32, n_tiles <= 2^24 / 16
+        w.acc_stride = 32;
+        while (w.acc_stride < p.nt) w.acc_stride <<= 1;
+        w.tmem_cols = 2 * w.acc_stride;
+        if (!r) r = launch_gemm_ws(th, tw, tout, w, s);
+    }
     give_back();
     return r;
 }

@@ -44,8 +44,8 @@ int kernel_from_env() {
 
 bool valid(int option, int v) {
     switch (option) {
-        case ACCSPMM_OPT_PACK: return v >= -1 && v <= 1;
-        case ACCSPMM_OPT_PREFETCH:
+        case ACCSPMM_OPT_PACK:
+        case ACCSPMM_OPT_PREFETCH: return v >= -1 && v <= 1;
         case ACCSPMM_OPT_SCHEDULE:
         case ACCSPMM_OPT_HOST_DIRECT_C: return v == 0 || v == 1;
         case ACCSPMM_OPT_SLICE_WIDTH:
@@ -67,7 +67,9 @@ void init_from_env() {
     // ACCSPMM_PACK: 0 never pack, 2 pack wherever the shape allows, else the rule
     const int pk = env_or("ACCSPMM_PACK", -1);
     g_opt[ACCSPMM_OPT_PACK] = pk == 0 ? 0 : pk == 2 ? 1 : -1;
-    g_opt[ACCSPMM_OPT_PREFETCH] = env_or("ACCSPMM_PREFETCH", 1) ? 1 : 0;
+    // ACCSPMM_PREFETCH: 0 never, 1 always, else the rule
+    const int pf = env_or("ACCSPMM_PREFETCH", -1);
+    g_opt[ACCSPMM_OPT_PREFETCH] = pf == 0 ? 0 : pf == 1 ? 1 : -1;
     g_opt[ACCSPMM_OPT_SCHEDULE] = env_or("ACCSPMM_SCHEDULE", 1) ? 1 : 0;
     g_opt[ACCSPMM_OPT_HOST_DIRECT_C] = env_or("ACCSPMM_HOST_DIRECT", 1) ? 1 : 0;
     const struct {

@@ -770,17 +770,22 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
         pack_tf32_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(B), static_cast<uint8_t*>(packed),
                                                 K, pitch, n4, static_cast<uint8_t*>(packed) + size_t(cols) * pitch);
         st = cudaGetLastError() == cudaSuccess ? ACCSPMM_SUCCESS : ACCSPMM_ERROR_CUDA;
-        // the B rows of the tile group two ahead are prefetched into L2
-        // (ACCSPMM_OPT_PREFETCH = 0 turns it off): 1.99 against 2.06 ms per
-        // step at K = 128, 3.82 against 4.01 ms at K = 256, bit-identical
+        // the B rows of the tile group two ahead are prefetched into L2,
+        // bit-identical; by default only when K spans an odd number of
+        // 128-column slices: on the 1M-row power-law matrix (adaptive step)
+        // the prefetch measured 1.643 against 1.667 ms at K = 128 and 4.64
+        // against 4.80 ms at K = 384, but 3.41 against 3.34 ms at K = 256,
+        // 3.31 against 3.24 at K = 192 and 6.71 against 6.57 at K = 512
+        const int pf_opt = option(ACCSPMM_OPT_PREFETCH);
+        const bool pf = pf_opt == 1 || (pf_opt < 0 && (a.n_slices & 1u));
         if (st == ACCSPMM_SUCCESS) {
 #ifdef ACCSPMM_LAB
-            if (option(ACCSPMM_OPT_PREFETCH) && lab_env("ACCSPMM_PFK", 2) == 1)
+            if (pf && lab_env("ACCSPMM_PFK", 2) == 1)
                 st = launch_packed_t<128, DirectBatch<128>::U, 2, true, 1>(a, s);
             else
 #endif
-            st = option(ACCSPMM_OPT_PREFETCH) ? launch_packed_t<128, DirectBatch<128>::U, 2, true>(a, s)
-                                              : launch_packed_t<128, DirectBatch<128>::U, 2>(a, s);
+            st = pf ? launch_packed_t<128, DirectBatch<128>::U, 2, true>(a, s)
+                    : launch_packed_t<128, DirectBatch<128>::U, 2>(a, s);
         }
         cudaFreeAsync(packed, s);
         if (st) ACC_FAIL(st, "packed SpMM launch failed");

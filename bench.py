@@ -195,7 +195,7 @@ def peaks():
 # the reason).
 KERNEL_SOURCES = ("accspmm_gb300/csrc/spmm.cu", "accspmm_gb300/csrc/spmm_direct.cuh",
                   "accspmm_gb300/csrc/spmm_common.cuh")
-TRAFFIC = {128: {"bytes": 8052258933, "src_sha": "98654848eac34155",
+TRAFFIC = {128: {"bytes": 8051474528, "src_sha": "b116fe8b843983cf",
                  "capture": "profiles/spmm_window_packed_kernel_powerlaw_local.md"}}
 
 

@@ -249,7 +249,8 @@ void accspmm_adpbme_destroy(accspmm_adpbme_t* adp);
  * 320 cols ceil(K / 128) bytes from the library's memory pool (released in
  * stream order): the SpMM then gathers 10 instead of 16 sectors of each
  * 128-column row slice, with bit-identical results, and prefetches into L2
- * the rows of the tile group two ahead of the one it loads.
+ * the rows of the tile group two ahead of the one it loads (when K spans an
+ * odd number of 128-column slices).
  * ACCSPMM_OPT_PACK and ACCSPMM_OPT_PREFETCH (accspmm_set_option) turn them
  * off or on. */
 int accspmm_spmm_tf32(const accspmm_metcf_t* metcf, const float* B, float* C,
@@ -448,9 +449,11 @@ enum {
                                          launches at 128-column slices pack a B of at least
                                          128 MiB to 2.5-byte TF32 rows first; 0 never; 1
                                          whenever the launch shape allows */
-    ACCSPMM_OPT_PREFETCH = 1,         /* ACCSPMM_PREFETCH: 1 (default) the packed kernel
-                                         prefetches into L2 the rows of the tile group two
-                                         ahead; 0 it does not */
+    ACCSPMM_OPT_PREFETCH = 1,         /* ACCSPMM_PREFETCH (0 -> 0, 1 -> 1): -1 (default)
+                                         the packed kernel prefetches into L2 the rows of
+                                         the tile group two ahead when K spans an odd
+                                         number of 128-column slices (where it measured
+                                         faster); 0 never; 1 always */
     ACCSPMM_OPT_SCHEDULE = 2,         /* ACCSPMM_SCHEDULE: 1 (default) launches of a few
                                          waves run their window blocks heaviest first; 0 in
                                          window order */

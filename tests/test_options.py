@@ -13,7 +13,7 @@ from accspmm_gb300 import capi
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
-DEFAULTS = {capi.OPT_PACK: -1, capi.OPT_PREFETCH: 1, capi.OPT_SCHEDULE: 1, capi.OPT_SLICE_WIDTH: 0,
+DEFAULTS = {capi.OPT_PACK: -1, capi.OPT_PREFETCH: -1, capi.OPT_SCHEDULE: 1, capi.OPT_SLICE_WIDTH: 0,
             capi.OPT_CTAS_PER_SM: 0, capi.OPT_TILE_RING: -1, capi.OPT_WINDOWS_PER_CTA: 0,
             capi.OPT_HOST_SLICE_WIDTH: 0, capi.OPT_HOST_DIRECT_C: 1, capi.OPT_KERNEL: 0}
 
@@ -55,7 +55,7 @@ def test_set_get_round_trip_and_refusals():
         capi.set_option(capi.OPT_SLICE_WIDTH, 32)
         assert capi.get_option(capi.OPT_SLICE_WIDTH) == 32
         for opt, val in ((capi.OPT_SLICE_WIDTH, 48), (capi.OPT_PACK, 2), (capi.OPT_TILE_RING, 3),
-                         (capi.OPT_WINDOWS_PER_CTA, 2000), (42, 0), (-1, 0)):
+                         (capi.OPT_WINDOWS_PER_CTA, 2000), (capi.OPT_PREFETCH, 2), (42, 0), (-1, 0)):
             assert lib.accspmm_set_option(opt, val) == capi.ERROR_INVALID_VALUE
         assert capi.get_option(capi.OPT_SLICE_WIDTH) == 32
         for k in ("pipe", "bulk", "lean", "db", "tma", "staged"):
