@@ -92,16 +92,7 @@ __global__ void pack_tf32_kernel(const float4* __restrict__ B, uint8_t* __restri
          i += size_t(gridDim.x) * blockDim.x) {
         const size_t row = i / k4;
         const uint32_t c = uint32_t(i - row * k4) * 4;
-        const float4 v = __ldcs(B + i);
-        const uint32_t r0 = f2tf32(v.x), r1 = f2tf32(v.y), r2 = f2tf32(v.z), r3 = f2tf32(v.w);
-        // slice c / 128 of the row: column group g = (c / 4) % 8, h = (c / 32) % 4
-        uint8_t* base = P + row * pitch + 320 * (c >> 7);
-        const uint32_t g = (c >> 2) & 7, h = (c >> 5) & 3;
-        *reinterpret_cast<uint2*>(base + 128 * (h >> 1) + 16 * g + 8 * (h & 1)) =
-            make_uint2((r0 >> 16) | (r1 & 0xFFFF0000u), (r2 >> 16) | (r3 & 0xFFFF0000u));
-        *reinterpret_cast<uint16_t*>(base + 256 + 8 * g + 2 * h) =
-            uint16_t(((r0 >> 8) & 0xF0u) | ((r1 >> 12) & 0x0Fu) | (((r2 >> 8) & 0xF0u) << 8) |
-                     (((r3 >> 12) & 0x0Fu) << 8));
+        pack_tf32_put(P + row * pitch, c, __ldcs(B + i));
     }
 }
 
@@ -745,16 +736,17 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     // TF32 at 128-column slices with the ring: B is first rounded to TF32 and
     // packed to 2.5 bytes a value (pack_tf32_kernel), so the SpMM gathers 10
     // of every 16 sectors of a row in 3 instead of 4 loads; the MMAs see the
-    // same operand bits, so the results are bit-identical.  On the 1M-row
-    // power-law matrix: 2.00 ms per call (packing included) against 2.30 ms
-    // at K = 128, 3.91 against 4.45 ms at K = 256; on the 2M-row GCN graph at
-    // K = 256 (a 2 GiB B) 6.95 against 7.46 ms.  The default rule packs a B of at least 128 MiB: at
-    // 64-column slices (K = 64) a 3-byte packing cost what the gathers saved,
-    // and a B that fits the L2 (the 16,384-row matrix, 53.5 against 52.0 us)
-    // only gains a pass.  The autotuner times both ways.
+    // same operand bits, so the results are bit-identical.  The default rule
+    // packs a B of at least 4 MiB; per adaptive call, packing included,
+    // against the same launch reading fp32 B: 1M-row power-law matrix 1.64
+    // against 2.29 ms at K = 128; 524,288 rows 0.85 against 1.23 ms (K = 128)
+    // and 1.68 against 2.30 ms (K = 256); 65,536 rows 111 against 164 us; the
+    // 16,384-row symmetric matrix (an 8 MiB B that fits the L2) 43.7 against
+    // 52.4 us.  (At 64-column slices, K = 64, a 3-byte packing cost what the
+    // gathers saved.)  The autotuner times both ways.
     const bool ring_on = cfg.ring != 0;
     const uint64_t b_bytes = uint64_t(cols) * K * 4;
-    const bool pack_rule = cfg.pack > 0 || (cfg.pack < 0 && b_bytes >= (uint64_t(128) << 20));
+    const bool pack_rule = cfg.pack > 0 || (cfg.pack < 0 && b_bytes >= (uint64_t(4) << 20));
     if (allow_pack && !x3 && !(epi.bias || epi.act) && ring_on && cfg.fs == 128 && occ == 2 && pack_rule) {
         cudaMemPool_t pool;
         int st = library_pool(&pool);
@@ -964,8 +956,8 @@ int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uin
 // the process exits.  All calls share the array, so calls that overlap on the
 // GPU (different streams, no ordering between them) race on it.  It never
 // packs B (that copy would need a scratch the size of B), so on a B of
-// 128 MiB or more at K > 64 it runs the kernel that reads fp32 B: the same
-// bits, 2.29 against 1.95 ms on the 1M-row power-law matrix at K = 128.
+// 4 MiB or more at K > 64 it runs the kernel that reads fp32 B: the same
+// bits, 2.29 against 1.64 ms on the 1M-row power-law matrix at K = 128.
 // ---------------------------------------------------------------------------
 constexpr uint32_t kNoAllocWords = 1u << 20;  // 4 MiB: windows + 2 words
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocWords];

@@ -9,10 +9,14 @@
 // first; resident CTAs take items from an atomic counter until none are
 // left, so uneven matrices share the GPU without a tail of idle SMs.  TF32
 // matrices with K > 64 form a second group launched in 128-column slices
-// with the rolling tile ring, their one-matrix default shape.
+// with the rolling tile ring, their one-matrix default shape; a plan packs the
+// B of those whose B is at least 4 MiB (the one-matrix rule) to 2.5-byte TF32
+// rows into a buffer it owns, with one launch over all of them before the
+// wide group runs, and their items read the packed rows (bit-identical).
 // A plan can be captured into a CUDA graph (counter reset + launch) and
 // replayed.
 #include <algorithm>
+#include <cstdint>
 #include <cstdlib>
 #include <numeric>
 #include <vector>
@@ -44,8 +48,11 @@ __device__ __forceinline__ uint32_t find_desc(const BatchDesc* __restrict__ d, u
 }
 
 // U tiles per gather batch and MINB resident CTAs per SM, as in the
-// one-matrix register-direct kernel's default shape.
-template <int FS, int PREC, int U, int MINB, bool ROLL>
+// one-matrix register-direct kernel's default shape.  PK: every item has a
+// packed B and runs the packed-B loop of the one-matrix packed kernel (with
+// the L2 prefetch when K spans an odd number of 128-column slices, the
+// one-matrix default); otherwise the fp32 loop.
+template <int FS, int PREC, int U, int MINB, bool ROLL, bool PK = false>
 __global__ void __launch_bounds__(kNW * 32, MINB)
 spmm_batch_kernel(const BatchDesc* __restrict__ desc, uint32_t n_desc, uint32_t total_items,
                   uint32_t* __restrict__ counter) {
@@ -64,7 +71,7 @@ spmm_batch_kernel(const BatchDesc* __restrict__ desc, uint32_t n_desc, uint32_t 
                 const uint32_t local = item - d.item0;
                 s_args = SpmmArgs{d.rwo, d.tc_offset, d.bits, d.a2b, d.vals, d.B, d.C, d.W, d.cols,
                                   d.K, d.wb, d.n_slices, d.n_wblocks, 0, 0, nullptr, 0, nullptr,
-                                  nullptr, 0};
+                                  PK ? d.bp : nullptr, PK ? d.bpitch : 0u};
                 s_wbk = local / d.n_slices;
                 s_slice = local - s_wbk * d.n_slices;
             }
@@ -73,12 +80,17 @@ spmm_batch_kernel(const BatchDesc* __restrict__ desc, uint32_t n_desc, uint32_t 
         if (s_item >= total_items) break;
         Block<FS, kNW> blk;
         blk.init_item(s_args, s_wbk, s_slice, s_rwo, part);
-        direct_item<FS, PREC, U, false, kNW, ROLL>(s_args, blk);
+        if constexpr (PK) {
+            if (s_args.n_slices & 1u) direct_item_packed<FS, U, kNW, true>(s_args, blk);
+            else direct_item_packed<FS, U, kNW, false>(s_args, blk);
+        } else {
+            direct_item<FS, PREC, U, false, kNW, ROLL>(s_args, blk);
+        }
         __syncthreads();  // s_args, s_rwo and the slots are reused by the next item
     }
 }
 
-template <int FS, int PREC, bool ROLL>
+template <int FS, int PREC, bool ROLL, bool PK = false>
 int launch_batch_t(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items,
                    uint32_t max_wb, uint32_t* d_counter, cudaStream_t s) {
     // 128-column slices: 2 CTAs per SM with the one-matrix kernel's batch;
@@ -90,16 +102,50 @@ int launch_batch_t(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_item
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 32 && !(attr_set & (1u << dev))) {
-        ACC_CUDA(cudaFuncSetAttribute(spmm_batch_kernel<FS, PREC, kU, kMinB, ROLL>,
+        ACC_CUDA(cudaFuncSetAttribute(spmm_batch_kernel<FS, PREC, kU, kMinB, ROLL, PK>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
         attr_set |= 1u << dev;
     }
     if (smem > 100 * 1024) ACC_FAIL(ACCSPMM_ERROR_UNSUPPORTED, "window block too large for a batch");
     const uint32_t grid = std::min<uint32_t>(total_items, uint32_t(sm_count()) * kMinB);
     if (grid == 0) return ACCSPMM_SUCCESS;
-    spmm_batch_kernel<FS, PREC, kU, kMinB, ROLL><<<grid, kNW * 32, smem, s>>>(d_desc, n_desc, total_items, d_counter);
+    spmm_batch_kernel<FS, PREC, kU, kMinB, ROLL, PK><<<grid, kNW * 32, smem, s>>>(d_desc, n_desc, total_items, d_counter);
     ACC_LAUNCH_CHECK();
     return ACCSPMM_SUCCESS;
+}
+
+// One matrix's B for the batched packing launch.
+struct PackDesc {
+    const float4* B;
+    uint8_t* P;        // packed rows, then the zero row
+    uint32_t K, pitch;
+    uint64_t start;    // first float4 of this B in the launch's numbering
+    uint64_t n4;       // float4s of this B
+};
+
+// Packs every listed B (pack_tf32_put layout) and writes each zero row; one
+// float4 of B per thread and step, read once with a streaming load.
+__global__ void pack_tf32_batch_kernel(const PackDesc* __restrict__ d, uint32_t n, uint64_t total) {
+    for (uint32_t j = blockIdx.x; j < n; j += gridDim.x) {
+        uint8_t* zero_row = d[j].P + (d[j].n4 / (d[j].K / 4)) * d[j].pitch;
+        for (uint32_t t = threadIdx.x; t < d[j].pitch / 8; t += blockDim.x)
+            reinterpret_cast<uint2*>(zero_row)[t] = make_uint2(0u, 0u);
+    }
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+         i += uint64_t(gridDim.x) * blockDim.x) {
+        uint32_t lo = 0, hi = n;  // last desc with start <= i
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) / 2;
+            if (d[mid].start <= i) lo = mid;
+            else hi = mid;
+        }
+        const PackDesc& x = d[lo];
+        const uint64_t local = i - x.start;
+        const uint32_t k4 = x.K / 4;
+        const uint64_t row = local / k4;
+        const uint32_t c = uint32_t(local - row * k4) * 4;
+        pack_tf32_put(x.P + row * x.pitch, c, __ldcs(x.B + local));
+    }
 }
 
 }  // namespace
@@ -117,7 +163,7 @@ bool batch_item_is_wide(uint32_t K, int precision) {
 }
 
 int launch_batch(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items, uint32_t max_wb,
-                 uint32_t* d_counter, int fs, int precision, cudaStream_t s) {
+                 uint32_t* d_counter, int fs, int precision, cudaStream_t s, bool packed) {
     ACC_CUDA(cudaMemsetAsync(d_counter, 0, 4, s));
     const bool x3 = precision == ACCSPMM_PREC_3XTF32;
     // the rolling tile ring spills in the persistent kernel (24 bytes) and
@@ -132,6 +178,8 @@ int launch_batch(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items,
         // wide TF32 items: 128-column slices with the rolling tile ring, the
         // one-matrix default for K > 64
         if (x3) ACC_FAIL(ACCSPMM_ERROR_UNSUPPORTED, "128-column batch slices are TF32 only");
+        if (packed)
+            return launch_batch_t<128, ACCSPMM_PREC_TF32, true, true>(d_desc, n_desc, total_items, max_wb, d_counter, s);
         return launch_batch_t<128, ACCSPMM_PREC_TF32, true>(d_desc, n_desc, total_items, max_wb, d_counter, s);
     }
     switch (fs) {
@@ -193,18 +241,26 @@ using namespace accspmm;
 // One persistent launch of a plan: the items of one slice-width class.
 struct BatchGroup {
     int fs = 64;
+    bool packed = false;  // every item reads a packed B
     uint32_t n_desc = 0, total_items = 0, max_wb = 1;
     BatchDesc* d_desc = nullptr;
     uint32_t* d_counter = nullptr;
 };
 
 // A plan: TF32 items with K > 64 run in 128-column slices with the tile ring
-// (the one-matrix default for them), the others in the narrow shape; one
-// persistent launch per non-empty group, wide group first.
+// (the one-matrix default for them) -- those whose B the one-matrix rule packs
+// in one group reading packed copies (after one packing launch), the rest in
+// a group reading fp32 B -- and the others in the narrow shape; one
+// persistent launch per non-empty group, wide groups first.
 struct accspmm_batch {
     int device = 0;
     int precision = ACCSPMM_PREC_TF32;
     std::vector<BatchGroup> groups;
+    // packed copies of the wide group's large B (owned), launched before it
+    uint8_t* d_packed = nullptr;
+    PackDesc* d_pack = nullptr;
+    uint32_t n_pack = 0;
+    uint64_t pack_total = 0;
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
 };
@@ -215,6 +271,53 @@ static void free_groups(accspmm_batch* b) {
         cudaFree(g.d_counter);
     }
     b->groups.clear();
+    cudaFree(b->d_packed);
+    cudaFree(b->d_pack);
+    b->d_packed = nullptr;
+    b->d_pack = nullptr;
+    b->n_pack = 0;
+}
+
+// Whether a wide item's B is packed: the one-matrix rule (a B of at least
+// 4 MiB, or as ACCSPMM_OPT_PACK says).
+static bool batch_item_packs(uint32_t cols, uint32_t K) {
+    const int pk = option(ACCSPMM_OPT_PACK);
+    const uint64_t b_bytes = uint64_t(cols) * K * 4;
+    return cols > 0 && (pk > 0 || (pk < 0 && b_bytes >= (uint64_t(4) << 20)));
+}
+
+// Packed copies of the B of every item in d, in one buffer owned by the
+// plan; points the descriptors at them.
+static int plan_packing(accspmm_batch* b, std::vector<BatchDesc>* d) {
+    std::vector<size_t> off(d->size(), SIZE_MAX);
+    size_t bytes = 0;
+    for (size_t i = 0; i < d->size(); ++i) {
+        const BatchDesc& x = (*d)[i];
+        if (x.cols == 0) continue;
+        off[i] = bytes;
+        const size_t pitch = 320 * ((x.K + 127) / 128);
+        bytes += ((size_t(x.cols) + 1) * pitch + 64 + 255) / 256 * 256;
+    }
+    if (bytes == 0) return ACCSPMM_SUCCESS;
+    if (cudaMalloc(&b->d_packed, bytes) != cudaSuccess)
+        ACC_FAIL(ACCSPMM_ERROR_ALLOC, "device allocation of the packed B copies (%zu bytes) failed", bytes);
+    std::vector<PackDesc> pd;
+    uint64_t start = 0;
+    for (size_t i = 0; i < d->size(); ++i) {
+        if (off[i] == SIZE_MAX) continue;
+        BatchDesc& x = (*d)[i];
+        x.bp = b->d_packed + off[i];
+        x.bpitch = 320 * ((x.K + 127) / 128);
+        const uint64_t n4 = uint64_t(x.cols) * (x.K / 4);
+        pd.push_back(PackDesc{reinterpret_cast<const float4*>(x.B), b->d_packed + off[i], x.K, x.bpitch, start, n4});
+        start += n4;
+    }
+    if (cudaMalloc(&b->d_pack, sizeof(PackDesc) * pd.size()) != cudaSuccess ||
+        cudaMemcpy(b->d_pack, pd.data(), sizeof(PackDesc) * pd.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        ACC_FAIL(ACCSPMM_ERROR_ALLOC, "device table of the packed B copies failed");
+    b->n_pack = uint32_t(pd.size());
+    b->pack_total = start;
+    return ACCSPMM_SUCCESS;
 }
 
 extern "C" {
@@ -237,20 +340,22 @@ int accspmm_batch_create(const accspmm_batch_item_t* items, uint32_t n, int32_t 
     auto* b = new accspmm_batch();
     cudaGetDevice(&b->device);
     b->precision = precision;
-    // split by slice-width class, keeping each item's position for its index
-    std::vector<BatchInput> cls[2];
-    std::vector<uint32_t> pos[2];
+    // split by class -- wide with packed B, wide reading fp32 B, narrow --
+    // keeping each item's position for its index
+    std::vector<BatchInput> cls[3];
+    std::vector<uint32_t> pos[3];
     uint32_t narrow_k = 4;
     for (uint32_t i = 0; i < n; ++i) {
-        const int c = batch_item_is_wide(in[i].K, precision) ? 0 : 1;
+        const int c = batch_item_is_wide(in[i].K, precision) ? (batch_item_packs(in[i].cols, in[i].K) ? 0 : 1) : 2;
         cls[c].push_back(in[i]);
         pos[c].push_back(i);
-        if (c == 1) narrow_k = std::max(narrow_k, in[i].K);
+        if (c == 2) narrow_k = std::max(narrow_k, in[i].K);
     }
-    for (int c = 0; c < 2; ++c) {
+    for (int c = 0; c < 3; ++c) {
         if (cls[c].empty()) continue;
         BatchGroup g;
-        g.fs = c == 0 ? 128 : batch_fs_for(narrow_k);
+        g.fs = c < 2 ? 128 : batch_fs_for(narrow_k);
+        g.packed = c == 0;
         std::vector<BatchDesc> d;
         int st = make_batch_descs(cls[c].data(), uint32_t(cls[c].size()), g.fs, precision, &d,
                                   &g.total_items, &g.max_wb);
@@ -260,6 +365,11 @@ int accspmm_batch_create(const accspmm_batch_item_t* items, uint32_t n, int32_t 
             return st;
         }
         for (auto& x : d) x.index = pos[c][x.index];
+        if (g.packed && (st = plan_packing(b, &d))) {
+            free_groups(b);
+            delete b;
+            return st;
+        }
         g.n_desc = uint32_t(d.size());
         if (cudaMalloc(&g.d_desc, sizeof(BatchDesc) * std::max<size_t>(1, d.size())) != cudaSuccess ||
             cudaMalloc(&g.d_counter, 4) != cudaSuccess) {
@@ -283,10 +393,17 @@ int accspmm_batch_create(const accspmm_batch_item_t* items, uint32_t n, int32_t 
 int accspmm_batch_run(accspmm_batch_t* b, void* stream) {
     clear_error();
     if (!b) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "null batch");
+    if (b->n_pack) {
+        // this run's B values, packed before the wide group reads them
+        const unsigned blocks = unsigned(std::min<uint64_t>((b->pack_total + 255) / 256 + 1,
+                                                            uint64_t(sm_count()) * 16));
+        pack_tf32_batch_kernel<<<blocks, 256, 0, as_stream(stream)>>>(b->d_pack, b->n_pack, b->pack_total);
+        ACC_LAUNCH_CHECK();
+    }
     for (const auto& g : b->groups) {
         if (g.total_items == 0) continue;
         const int st = launch_batch(g.d_desc, g.n_desc, g.total_items, g.max_wb, g.d_counter, g.fs,
-                                    b->precision, as_stream(stream));
+                                    b->precision, as_stream(stream), g.packed);
         if (st) return st;
     }
     return ACCSPMM_SUCCESS;

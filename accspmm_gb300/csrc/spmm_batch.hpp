@@ -24,6 +24,8 @@ struct BatchDesc {
     uint32_t wb, n_slices, n_wblocks;  // launch shape of this matrix
     uint32_t item0;                    // first work item of this matrix
     uint32_t index;                    // position in the caller's list
+    const uint8_t* bp;                 // B packed to TF32 (pack_tf32_put layout), or nullptr
+    uint32_t bpitch;                   // bytes per packed row
 };
 
 // Host description of one matrix of a batch.
@@ -52,7 +54,8 @@ int make_batch_descs(const BatchInput* in, uint32_t n, int fs, int precision,
                      std::vector<BatchDesc>* out, uint32_t* total_items, uint32_t* max_wb);
 
 // Resets the work counter and launches the persistent batched kernel.
+// packed: every descriptor has a packed B (wide TF32 group only).
 int launch_batch(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items, uint32_t max_wb,
-                 uint32_t* d_counter, int fs, int precision, cudaStream_t s);
+                 uint32_t* d_counter, int fs, int precision, cudaStream_t s, bool packed = false);
 
 }  // namespace accspmm

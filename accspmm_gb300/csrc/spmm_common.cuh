@@ -35,10 +35,10 @@ struct SpmmArgs {
     // (No default member initializer: the batched kernel keeps a SpmmArgs in
     // shared memory; brace initialisation without it leaves it null.)
     const uint32_t* order;
-    // B rounded to TF32 and packed (pack_tf32_kernel): row i at bp + i * bpitch
-    // bytes holds bits 31..16 of its K values as K halfwords, then bits 15..8
-    // (only 15..13 can be set) as K bytes, so a gathered row is one contiguous
-    // run.  nullptr: the kernels read B.
+    // B rounded to TF32 and packed to 2.5 bytes a value (pack_tf32_put): row
+    // i at bp + i * bpitch bytes, 320 bytes per 128-column slice (halfwords of
+    // bits 31..16, then nibbles of bits 15..12), and a zero row at index cols
+    // that padding entries read.  nullptr: the kernels read B.
     const uint8_t* bp;
     uint32_t bpitch;
 };

@@ -178,6 +178,23 @@ __device__ __forceinline__ void direct_item(const SpmmArgs& a, const Block<FS, N
 // whose products land only in columns that are not stored): 8 % fewer
 // instructions and 5 % less time than predicated loads on the 1M-row
 // power-law matrix at K = 128 and 256.
+// One float4 of B (columns c .. c + 3 of a row, c % 4 == 0) rounded to TF32
+// and stored into the row's packed form at `row` (320 bytes per 128-column
+// slice: the halfwords of bits 31..16 ordered so that each lane's 8 values
+// are two runs of 16 bytes, then the nibbles of bits 15..12, 8 bytes per
+// lane); the layout direct_item_packed reads.
+__device__ __forceinline__ void pack_tf32_put(uint8_t* row, uint32_t c, float4 v) {
+    const uint32_t r0 = f2tf32(v.x), r1 = f2tf32(v.y), r2 = f2tf32(v.z), r3 = f2tf32(v.w);
+    // slice c / 128 of the row: column group g = (c / 4) % 8, h = (c / 32) % 4
+    uint8_t* base = row + 320 * (c >> 7);
+    const uint32_t g = (c >> 2) & 7, h = (c >> 5) & 3;
+    *reinterpret_cast<uint2*>(base + 128 * (h >> 1) + 16 * g + 8 * (h & 1)) =
+        make_uint2((r0 >> 16) | (r1 & 0xFFFF0000u), (r2 >> 16) | (r3 & 0xFFFF0000u));
+    *reinterpret_cast<uint16_t*>(base + 256 + 8 * g + 2 * h) =
+        uint16_t(((r0 >> 8) & 0xF0u) | ((r1 >> 12) & 0x0Fu) | (((r2 >> 8) & 0xF0u) << 8) |
+                 (((r3 >> 12) & 0x0Fu) << 8));
+}
+
 // PFK: how rows are prefetched -- 1 one cp.async.bulk.prefetch.L2 of the
 // 320-byte slice per row (its address operand is uniform, so the lanes'
 // prefetches issue one after another), 2 three prefetch.global.L2 of the

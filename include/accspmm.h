@@ -244,7 +244,7 @@ void accspmm_adpbme_destroy(accspmm_adpbme_t* adp);
  * schedule until accspmm_metcf_destroy (results do not depend on it).
  * Calls may be captured into a CUDA graph; a call captured before the
  * schedule exists runs the blocks in window order.  In TF32 with K > 64 and
- * a B of at least 128 MiB (or as a tuned shape says) a call first rounds B
+ * a B of at least 4 MiB (or as a tuned shape says) a call first rounds B
  * to TF32 and packs each row to 2.5 bytes a value in a buffer of
  * 320 cols ceil(K / 128) bytes from the library's memory pool (released in
  * stream order): the SpMM then gathers 10 instead of 16 sectors of each
@@ -369,8 +369,8 @@ int accspmm_spmm_host(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp,
  * same bits; rowIndices are checked in stream order and inconsistencies are
  * reported by accspmm_device_status, as for a caller-filled AdpBME there.
  * Unlike accspmm_spmm_adaptive it never packs B (the packed copy would need
- * 320 cols ceil(K / 128) bytes of scratch): on a B of 128 MiB or more at
- * K > 64 it runs the kernel that reads fp32 B, 2.29 against 1.95 ms per call
+ * 320 cols ceil(K / 128) bytes of scratch): on a B of 4 MiB or more at
+ * K > 64 it runs the kernel that reads fp32 B, 2.29 against 1.64 ms per call
  * on the 1M-row power-law matrix at K = 128 (GB300). */
 int accspmm_spmm_adaptive_noalloc(const accspmm_adpbme_t* adp, const float* B,
                                   float* C, uint32_t c_rows, uint32_t K,
@@ -447,7 +447,7 @@ void accspmm_autotune_clear(void);
 enum {
     ACCSPMM_OPT_PACK = 0,             /* ACCSPMM_PACK (0 -> 0, 2 -> 1): -1 (default) TF32
                                          launches at 128-column slices pack a B of at least
-                                         128 MiB to 2.5-byte TF32 rows first; 0 never; 1
+                                         4 MiB to 2.5-byte TF32 rows first; 0 never; 1
                                          whenever the launch shape allows */
     ACCSPMM_OPT_PREFETCH = 1,         /* ACCSPMM_PREFETCH (0 -> 0, 1 -> 1): -1 (default)
                                          the packed kernel prefetches into L2 the rows of

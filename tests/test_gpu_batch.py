@@ -106,3 +106,29 @@ def test_batch_rejects_bad_items():
         api.Batch([(m, B, C, 30)])
     with pytest.raises(capi.AccSpmmError):
         api.Batch([(m, B.data_ptr() + 4, C, 64)])
+
+
+def test_batch_with_packed_b_matches_plain_bitwise():
+    """Wide TF32 items whose B the plan packs (all of them with
+    ACCSPMM_OPT_PACK = 1, small ones included) run in their own persistent
+    launch over packed copies the plan owns, packed again on every run: the
+    results equal one plain launch per matrix bit for bit, also from a graph
+    replay after B has changed."""
+    with capi.option(capi.OPT_PACK, 1):
+        items = build_items((128, 200, 64))
+        ref = plain_results(items, capi.PREC_TF32)
+        b = api.Batch(items)
+        s = torch.cuda.Stream()
+        b.run(s)
+        s.synchronize()
+        for (_, _, C, _), r in zip(items, ref):
+            np.testing.assert_array_equal(C.cpu().numpy(), r)
+        b.capture(s)
+        for _, B, C, _ in items:
+            B.mul_(2.0)
+            C.fill_(float("nan"))
+        torch.cuda.synchronize()
+        b.launch_graph(s)
+        s.synchronize()
+        for (_, _, C, _), r in zip(items, ref):
+            np.testing.assert_array_equal(C.cpu().numpy(), 2.0 * r)

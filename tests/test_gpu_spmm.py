@@ -649,7 +649,7 @@ def test_packed_b_with_prefetch_is_bit_identical_at_full_size():
 
 @pytest.mark.parametrize("K", [136, 256])
 def test_packed_b_is_bit_identical(K):
-    """TF32 launches at 128-column slices whose B is at least 128 MiB first
+    """TF32 launches at 128-column slices whose B is at least 4 MiB first
     pack B to 2.5 bytes a value (rounded to TF32; each 128-column slice of a
     row its halfwords of bits 31..16, then the nibbles of bits 15..12); the
     SpMM on the packed copy returns bitwise what
@@ -684,7 +684,7 @@ def test_packed_b_is_bit_identical(K):
 @pytest.mark.parametrize("K", [72, 128, 200])
 def test_forced_packing_on_a_small_b_is_bit_identical(K):
     """ACCSPMM_OPT_PACK = 1 packs B wherever the launch shape allows, also below the
-    default rule's 128 MiB: ragged last slices (K = 72, 200), rows that are
+    default rule's 4 MiB: ragged last slices (K = 72, 200), rows that are
     not a multiple of the window height, the plain and adaptive entry points."""
     n = 5003
     rp, ci, vals = synth.powerlaw_local(n=n, seed=7)
