@@ -80,7 +80,9 @@ __global__ void __launch_bounds__(NW * 32, MINB) spmm_window_packed_kernel(const
 // 128 hp + 16 g (one 16-byte load each), and bits 15..12 of all 16 values
 // are 8 adjacent nibble bytes at 256 + 8 g (one 8-byte load), byte 2h + j / 2
 // holding value j's bits in its high nibble for even j, low nibble for odd.
-// One float4 of B per thread and step, read once with a streaming load.
+// One float4 of B per thread and step, read once with a streaming load.  (FS
+// = 64: the same layout in 160-byte slices of 64 columns, pack_tf32_put.)
+template <int FS = 128>
 __global__ void pack_tf32_kernel(const float4* __restrict__ B, uint8_t* __restrict__ P, uint32_t K,
                                  uint32_t pitch, size_t n4, uint8_t* __restrict__ zero_row) {
     const uint32_t k4 = K / 4;
@@ -92,7 +94,7 @@ __global__ void pack_tf32_kernel(const float4* __restrict__ B, uint8_t* __restri
          i += size_t(gridDim.x) * blockDim.x) {
         const size_t row = i / k4;
         const uint32_t c = uint32_t(i - row * k4) * 4;
-        pack_tf32_put(P + row * pitch, c, __ldcs(B + i));
+        pack_tf32_put<FS>(P + row * pitch, c, __ldcs(B + i));
     }
 }
 
@@ -747,11 +749,22 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     const bool ring_on = cfg.ring != 0;
     const uint64_t b_bytes = uint64_t(cols) * K * 4;
     const bool pack_rule = cfg.pack > 0 || (cfg.pack < 0 && b_bytes >= (uint64_t(4) << 20));
-    if (allow_pack && !x3 && !(epi.bias || epi.act) && ring_on && cfg.fs == 128 && occ == 2 && pack_rule) {
+    const bool wide_pack = cfg.fs == 128 && occ == 2 && pack_rule;
+    // 64-column slices at 3 CTAs per SM (the default for 32 < K <= 64):
+    // 160-byte packed slices of 64 columns, by default for 48 < K <= 64 with a
+    // B of at least 4 MiB: adaptive step, packing included, at K = 64 1.07
+    // against 1.27 ms on the 1M-row power-law matrix, 255 against 326 us on
+    // 262,144 rows, 78 against 102 us on 65,536, 30.9 against 33.1 us on the
+    // 16,384-row matrix; at K = 48 (a packed slice still holds 64 columns)
+    // 1.07 against 1.08 ms on 1M rows but 30.2 against 28.0 us on 16K rows
+    const bool narrow_pack = cfg.fs == 64 && occ == 3 &&
+                             (cfg.pack > 0 || (cfg.pack < 0 && K > 48 && K <= 64 && b_bytes >= (uint64_t(4) << 20)));
+    if (allow_pack && !x3 && !(epi.bias || epi.act) && ring_on && (wide_pack || narrow_pack)) {
         cudaMemPool_t pool;
         int st = library_pool(&pool);
         if (st) return st;
-        const uint32_t pitch = 320 * ((K + 127) / 128);
+        const uint32_t fs = uint32_t(cfg.fs);
+        const uint32_t pitch = (fs * 5 / 2) * ((K + fs - 1) / fs);
         void* packed = nullptr;
         ACC_CUDA(cudaMallocFromPoolAsync(&packed, (size_t(cols) + 1) * pitch + 64, pool, s));
         a.bp = static_cast<const uint8_t*>(packed);
@@ -759,8 +772,12 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
         const size_t n4 = size_t(cols) * (K / 4);
         const unsigned blocks = unsigned(std::min<size_t>((n4 + 255) / 256 + 1, size_t(sm_count()) * 16));
         // the packed rows, then the zero row at index cols that padding reads
-        pack_tf32_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(B), static_cast<uint8_t*>(packed),
-                                                K, pitch, n4, static_cast<uint8_t*>(packed) + size_t(cols) * pitch);
+        if (fs == 64)
+            pack_tf32_kernel<64><<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(B), static_cast<uint8_t*>(packed),
+                                                        K, pitch, n4, static_cast<uint8_t*>(packed) + size_t(cols) * pitch);
+        else
+            pack_tf32_kernel<128><<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(B), static_cast<uint8_t*>(packed),
+                                                         K, pitch, n4, static_cast<uint8_t*>(packed) + size_t(cols) * pitch);
         st = cudaGetLastError() == cudaSuccess ? ACCSPMM_SUCCESS : ACCSPMM_ERROR_CUDA;
         // the B rows of the tile group two ahead are prefetched into L2,
         // bit-identical; by default only when K spans an odd number of
@@ -770,7 +787,11 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
         // 3.31 against 3.24 at K = 192 and 6.71 against 6.57 at K = 512
         const int pf_opt = option(ACCSPMM_OPT_PREFETCH);
         const bool pf = pf_opt == 1 || (pf_opt < 0 && (a.n_slices & 1u));
-        if (st == ACCSPMM_SUCCESS) {
+        if (st == ACCSPMM_SUCCESS && fs == 64) {
+            // two tiles in flight per warp at 3 CTAs per SM, the unpacked
+            // 64-column default's shape
+            st = launch_packed_t<64, 2, 3>(a, s);
+        } else if (st == ACCSPMM_SUCCESS) {
 #ifdef ACCSPMM_LAB
             if (pf && lab_env("ACCSPMM_PFK", 2) == 1)
                 st = launch_packed_t<128, DirectBatch<128>::U, 2, true, 1>(a, s);
@@ -956,7 +977,7 @@ int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uin
 // the process exits.  All calls share the array, so calls that overlap on the
 // GPU (different streams, no ordering between them) race on it.  It never
 // packs B (that copy would need a scratch the size of B), so on a B of
-// 4 MiB or more at K > 64 it runs the kernel that reads fp32 B: the same
+// 4 MiB or more at K > 48 it runs the kernel that reads fp32 B: the same
 // bits, 2.29 against 1.64 ms on the 1M-row power-law matrix at K = 128.
 // ---------------------------------------------------------------------------
 constexpr uint32_t kNoAllocWords = 1u << 20;  // 4 MiB: windows + 2 words
@@ -1047,8 +1068,10 @@ int autotune_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K
                 c.slice_major = 0;
                 c.pack = 0;
                 cand.push_back(c);
-                // TF32 with the ring at 128-column slices: also gathering from a packed B
-                if (precision == ACCSPMM_PREC_TF32 && c.kernel == kDirect && c.occ == 2 && c.ring == 1 && fs == 128) {
+                // TF32 with the ring at 128-column slices (2 CTAs per SM) or 64 (3):
+                // also gathering from a packed B
+                if (precision == ACCSPMM_PREC_TF32 && c.kernel == kDirect && c.ring == 1 &&
+                    ((fs == 128 && c.occ == 2) || (fs == 64 && c.occ == 3))) {
                     c.pack = 1;
                     cand.push_back(c);
                 }

@@ -10,9 +10,9 @@
 // left, so uneven matrices share the GPU without a tail of idle SMs.  TF32
 // matrices with K > 64 form a second group launched in 128-column slices
 // with the rolling tile ring, their one-matrix default shape; a plan packs the
-// B of those whose B is at least 4 MiB (the one-matrix rule) to 2.5-byte TF32
-// rows into a buffer it owns, with one launch over all of them before the
-// wide group runs, and their items read the packed rows (bit-identical).
+// B that the one-matrix rule packs (TF32, at least 4 MiB, K > 48) to 2.5-byte
+// TF32 rows into buffers it owns, with one launch over all of them before the
+// groups run, and their items read the packed rows (bit-identical).
 // A plan can be captured into a CUDA graph (counter reset + launch) and
 // replayed.
 #include <algorithm>
@@ -80,9 +80,11 @@ spmm_batch_kernel(const BatchDesc* __restrict__ desc, uint32_t n_desc, uint32_t 
         if (s_item >= total_items) break;
         Block<FS, kNW> blk;
         blk.init_item(s_args, s_wbk, s_slice, s_rwo, part);
-        if constexpr (PK) {
+        if constexpr (PK && FS == 128) {
             if (s_args.n_slices & 1u) direct_item_packed<FS, U, kNW, true>(s_args, blk);
             else direct_item_packed<FS, U, kNW, false>(s_args, blk);
+        } else if constexpr (PK) {
+            direct_item_packed<FS, U, kNW, false>(s_args, blk);
         } else {
             direct_item<FS, PREC, U, false, kNW, ROLL>(s_args, blk);
         }
@@ -119,6 +121,7 @@ struct PackDesc {
     const float4* B;
     uint8_t* P;        // packed rows, then the zero row
     uint32_t K, pitch;
+    uint32_t fs;       // slice width of the packed layout: 128 or 64
     uint64_t start;    // first float4 of this B in the launch's numbering
     uint64_t n4;       // float4s of this B
 };
@@ -144,7 +147,8 @@ __global__ void pack_tf32_batch_kernel(const PackDesc* __restrict__ d, uint32_t 
         const uint32_t k4 = x.K / 4;
         const uint64_t row = local / k4;
         const uint32_t c = uint32_t(local - row * k4) * 4;
-        pack_tf32_put(x.P + row * x.pitch, c, __ldcs(x.B + local));
+        if (x.fs == 64) pack_tf32_put<64>(x.P + row * x.pitch, c, __ldcs(x.B + local));
+        else pack_tf32_put<128>(x.P + row * x.pitch, c, __ldcs(x.B + local));
     }
 }
 
@@ -181,6 +185,11 @@ int launch_batch(const BatchDesc* d_desc, uint32_t n_desc, uint32_t total_items,
         if (packed)
             return launch_batch_t<128, ACCSPMM_PREC_TF32, true, true>(d_desc, n_desc, total_items, max_wb, d_counter, s);
         return launch_batch_t<128, ACCSPMM_PREC_TF32, true>(d_desc, n_desc, total_items, max_wb, d_counter, s);
+    }
+    if (packed) {
+        // narrow TF32 items over 160-byte packed slices of 64 columns
+        if (fs != 64 || x3) ACC_FAIL(ACCSPMM_ERROR_UNSUPPORTED, "packed narrow batch slices are 64-column TF32");
+        return launch_batch_t<64, ACCSPMM_PREC_TF32, false, true>(d_desc, n_desc, total_items, max_wb, d_counter, s);
     }
     switch (fs) {
         case 32: return x3 ? launch_batch_t<32, ACCSPMM_PREC_3XTF32, false>(d_desc, n_desc, total_items, max_wb, d_counter, s)
@@ -248,16 +257,19 @@ struct BatchGroup {
 };
 
 // A plan: TF32 items with K > 64 run in 128-column slices with the tile ring
-// (the one-matrix default for them) -- those whose B the one-matrix rule packs
-// in one group reading packed copies (after one packing launch), the rest in
-// a group reading fp32 B -- and the others in the narrow shape; one
-// persistent launch per non-empty group, wide groups first.
+// (the one-matrix default for them), the others in the narrow shape; in each,
+// the items whose B the one-matrix rule packs form a group of their own that
+// reads packed copies (128- or 64-column slices, written by one packing
+// launch at the start of each run); one persistent launch per non-empty
+// group, wide groups first.
 struct accspmm_batch {
     int device = 0;
     int precision = ACCSPMM_PREC_TF32;
     std::vector<BatchGroup> groups;
-    // packed copies of the wide group's large B (owned), launched before it
-    uint8_t* d_packed = nullptr;
+    // packed copies of the packed groups' B (owned, one buffer per group),
+    // all written by one launch at the start of a run
+    std::vector<void*> packed_bufs;
+    std::vector<PackDesc> pack_host;
     PackDesc* d_pack = nullptr;
     uint32_t n_pack = 0;
     uint64_t pack_total = 0;
@@ -271,52 +283,64 @@ static void free_groups(accspmm_batch* b) {
         cudaFree(g.d_counter);
     }
     b->groups.clear();
-    cudaFree(b->d_packed);
+    for (void* p : b->packed_bufs) cudaFree(p);
+    b->packed_bufs.clear();
+    b->pack_host.clear();
     cudaFree(b->d_pack);
-    b->d_packed = nullptr;
     b->d_pack = nullptr;
     b->n_pack = 0;
+    b->pack_total = 0;
 }
 
-// Whether a wide item's B is packed: the one-matrix rule (a B of at least
-// 4 MiB, or as ACCSPMM_OPT_PACK says).
-static bool batch_item_packs(uint32_t cols, uint32_t K) {
+// Whether an item's B is packed: the one-matrix rule -- TF32, a B of at
+// least 4 MiB, K > 64 (128-column slices) or 48 < K <= 64 (64-column slices),
+// or as ACCSPMM_OPT_PACK says (1: every TF32 item with K > 32).
+static bool batch_item_packs(uint32_t cols, uint32_t K, int precision) {
+    if (precision != ACCSPMM_PREC_TF32 || cols == 0 || K <= 32) return false;
     const int pk = option(ACCSPMM_OPT_PACK);
     const uint64_t b_bytes = uint64_t(cols) * K * 4;
-    return cols > 0 && (pk > 0 || (pk < 0 && b_bytes >= (uint64_t(4) << 20)));
+    return pk > 0 || (pk < 0 && K > 48 && b_bytes >= (uint64_t(4) << 20));
 }
 
-// Packed copies of the B of every item in d, in one buffer owned by the
-// plan; points the descriptors at them.
-static int plan_packing(accspmm_batch* b, std::vector<BatchDesc>* d) {
+// Packed copies (FS-column layout) of the B of every item in d, in one buffer
+// owned by the plan; points the descriptors at them and lists them for the
+// packing launch (upload_packing puts the list on the device).
+static int plan_packing(accspmm_batch* b, std::vector<BatchDesc>* d, uint32_t fs) {
     std::vector<size_t> off(d->size(), SIZE_MAX);
     size_t bytes = 0;
     for (size_t i = 0; i < d->size(); ++i) {
         const BatchDesc& x = (*d)[i];
         if (x.cols == 0) continue;
         off[i] = bytes;
-        const size_t pitch = 320 * ((x.K + 127) / 128);
+        const size_t pitch = size_t(fs * 5 / 2) * ((x.K + fs - 1) / fs);
         bytes += ((size_t(x.cols) + 1) * pitch + 64 + 255) / 256 * 256;
     }
     if (bytes == 0) return ACCSPMM_SUCCESS;
-    if (cudaMalloc(&b->d_packed, bytes) != cudaSuccess)
+    void* buf = nullptr;
+    if (cudaMalloc(&buf, bytes) != cudaSuccess)
         ACC_FAIL(ACCSPMM_ERROR_ALLOC, "device allocation of the packed B copies (%zu bytes) failed", bytes);
-    std::vector<PackDesc> pd;
-    uint64_t start = 0;
+    b->packed_bufs.push_back(buf);
+    uint8_t* base = static_cast<uint8_t*>(buf);
     for (size_t i = 0; i < d->size(); ++i) {
         if (off[i] == SIZE_MAX) continue;
         BatchDesc& x = (*d)[i];
-        x.bp = b->d_packed + off[i];
-        x.bpitch = 320 * ((x.K + 127) / 128);
+        x.bp = base + off[i];
+        x.bpitch = (fs * 5 / 2) * ((x.K + fs - 1) / fs);
         const uint64_t n4 = uint64_t(x.cols) * (x.K / 4);
-        pd.push_back(PackDesc{reinterpret_cast<const float4*>(x.B), b->d_packed + off[i], x.K, x.bpitch, start, n4});
-        start += n4;
+        b->pack_host.push_back(PackDesc{reinterpret_cast<const float4*>(x.B), base + off[i], x.K, x.bpitch, fs,
+                                        b->pack_total, n4});
+        b->pack_total += n4;
     }
-    if (cudaMalloc(&b->d_pack, sizeof(PackDesc) * pd.size()) != cudaSuccess ||
-        cudaMemcpy(b->d_pack, pd.data(), sizeof(PackDesc) * pd.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return ACCSPMM_SUCCESS;
+}
+
+static int upload_packing(accspmm_batch* b) {
+    if (b->pack_host.empty()) return ACCSPMM_SUCCESS;
+    const size_t bytes = sizeof(PackDesc) * b->pack_host.size();
+    if (cudaMalloc(&b->d_pack, bytes) != cudaSuccess ||
+        cudaMemcpy(b->d_pack, b->pack_host.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess)
         ACC_FAIL(ACCSPMM_ERROR_ALLOC, "device table of the packed B copies failed");
-    b->n_pack = uint32_t(pd.size());
-    b->pack_total = start;
+    b->n_pack = uint32_t(b->pack_host.size());
     return ACCSPMM_SUCCESS;
 }
 
@@ -340,22 +364,24 @@ int accspmm_batch_create(const accspmm_batch_item_t* items, uint32_t n, int32_t 
     auto* b = new accspmm_batch();
     cudaGetDevice(&b->device);
     b->precision = precision;
-    // split by class -- wide with packed B, wide reading fp32 B, narrow --
-    // keeping each item's position for its index
-    std::vector<BatchInput> cls[3];
-    std::vector<uint32_t> pos[3];
+    // split by class -- wide with packed B, wide reading fp32 B, narrow with
+    // packed B (64-column slices), narrow reading fp32 B -- keeping each
+    // item's position for its index
+    std::vector<BatchInput> cls[4];
+    std::vector<uint32_t> pos[4];
     uint32_t narrow_k = 4;
     for (uint32_t i = 0; i < n; ++i) {
-        const int c = batch_item_is_wide(in[i].K, precision) ? (batch_item_packs(in[i].cols, in[i].K) ? 0 : 1) : 2;
+        const bool packs = batch_item_packs(in[i].cols, in[i].K, precision);
+        const int c = batch_item_is_wide(in[i].K, precision) ? (packs ? 0 : 1) : (packs ? 2 : 3);
         cls[c].push_back(in[i]);
         pos[c].push_back(i);
-        if (c == 2) narrow_k = std::max(narrow_k, in[i].K);
+        if (c == 3) narrow_k = std::max(narrow_k, in[i].K);
     }
-    for (int c = 0; c < 3; ++c) {
+    for (int c = 0; c < 4; ++c) {
         if (cls[c].empty()) continue;
         BatchGroup g;
-        g.fs = c < 2 ? 128 : batch_fs_for(narrow_k);
-        g.packed = c == 0;
+        g.fs = c < 2 ? 128 : c == 2 ? 64 : batch_fs_for(narrow_k);
+        g.packed = c == 0 || c == 2;
         std::vector<BatchDesc> d;
         int st = make_batch_descs(cls[c].data(), uint32_t(cls[c].size()), g.fs, precision, &d,
                                   &g.total_items, &g.max_wb);
@@ -365,7 +391,7 @@ int accspmm_batch_create(const accspmm_batch_item_t* items, uint32_t n, int32_t 
             return st;
         }
         for (auto& x : d) x.index = pos[c][x.index];
-        if (g.packed && (st = plan_packing(b, &d))) {
+        if (g.packed && (st = plan_packing(b, &d, uint32_t(g.fs)))) {
             free_groups(b);
             delete b;
             return st;
@@ -385,6 +411,11 @@ int accspmm_batch_create(const accspmm_batch_item_t* items, uint32_t n, int32_t 
             delete b;
             ACC_FAIL(ACCSPMM_ERROR_CUDA, "copy of the batch table failed");
         }
+    }
+    if (const int st = upload_packing(b)) {
+        free_groups(b);
+        delete b;
+        return st;
     }
     *out = b;
     return ACCSPMM_SUCCESS;

@@ -88,11 +88,11 @@ __device__ __forceinline__ float comp(const float4& v, int j) {
     return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w;
 }
 
-// Packed TF32 B at 128-column slices (pack_tf32_kernel).  For one gathered
-// row a lane of column group g holds hw[h] = bits 31..16 of values
-// 32h + 4g + 0..3 (two to a word, h = 0..3) and nb = 8 nibble bytes: byte
-// 2h + (j >> 1) holds bits 15..12 of value 32h + 4g + j, even j in the high
-// nibble.  Word hp of nb covers h = 2hp and 2hp + 1.
+// Packed TF32 B at 128- or 64-column slices (pack_tf32_put).  For one
+// gathered row a lane of column group g holds hw[h] = bits 31..16 of values
+// 32h + 4g + 0..3 (two to a word, h < FS / 32) and nb = FS / 16 nibble
+// bytes: byte 2h + (j >> 1) holds bits 15..12 of value 32h + 4g + j, even j
+// in the high nibble.  Word hp of nb covers h = 2hp and 2hp + 1.
 __device__ __forceinline__ uint4 ldg_u4_ordered(const uint8_t* p) {
     uint4 v;
     asm volatile("ld.global.nc.v4.u32 {%0, %1, %2, %3}, [%4];"
@@ -104,6 +104,12 @@ __device__ __forceinline__ uint4 ldg_u4_ordered(const uint8_t* p) {
 __device__ __forceinline__ uint2 ldg_u2_ordered(const uint8_t* p) {
     uint2 v;
     asm volatile("ld.global.nc.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ uint32_t ldg_u32_ordered(const uint8_t* p) {
+    uint32_t v;
+    asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(v) : "l"(p));
     return v;
 }
 
@@ -207,7 +213,7 @@ __device__ __forceinline__ void tile_mma(float (&acc)[Layout<H>::NM][4], const f
 template <int H>
 __device__ __forceinline__ void tile_mma_packed(float (&acc)[Layout<H>::NM][4], const uint2 (&h0)[H], uint2 n0,
                                                 const uint2 (&h1)[H], uint2 n1, float av0, float av1) {
-    static_assert(H == 4, "packed B is gathered at 128-column slices");
+    static_assert(H == 4 || H == 2, "packed B is gathered at 128- or 64-column slices");
     constexpr int NM = Layout<H>::NM;
     const uint32_t b0 = f2tf32(av0), b1 = f2tf32(av1);
     const uint32_t n0s[2] = {n0.x << 4, n0.y << 4}, n1s[2] = {n1.x << 4, n1.y << 4};

@@ -179,18 +179,23 @@ __device__ __forceinline__ void direct_item(const SpmmArgs& a, const Block<FS, N
 // instructions and 5 % less time than predicated loads on the 1M-row
 // power-law matrix at K = 128 and 256.
 // One float4 of B (columns c .. c + 3 of a row, c % 4 == 0) rounded to TF32
-// and stored into the row's packed form at `row` (320 bytes per 128-column
-// slice: the halfwords of bits 31..16 ordered so that each lane's 8 values
-// are two runs of 16 bytes, then the nibbles of bits 15..12, 8 bytes per
-// lane); the layout direct_item_packed reads.
+// and stored into the row's packed form at `row`, the layout
+// direct_item_packed reads.  A row is cut into FS-column slices of
+// FS * 5 / 2 bytes (320 at FS = 128, 160 at FS = 64): the halfwords of bits
+// 31..16 of the slice's values (2 FS bytes), ordered so that each lane's
+// values come in runs of 16 bytes, then the nibbles of bits 15..12 (FS / 2
+// bytes, FS / 16 per lane).
+template <int FS = 128>
 __device__ __forceinline__ void pack_tf32_put(uint8_t* row, uint32_t c, float4 v) {
+    static_assert(FS == 128 || FS == 64, "packed slices are 128 or 64 columns");
+    constexpr uint32_t H = FS / 32;
     const uint32_t r0 = f2tf32(v.x), r1 = f2tf32(v.y), r2 = f2tf32(v.z), r3 = f2tf32(v.w);
-    // slice c / 128 of the row: column group g = (c / 4) % 8, h = (c / 32) % 4
-    uint8_t* base = row + 320 * (c >> 7);
-    const uint32_t g = (c >> 2) & 7, h = (c >> 5) & 3;
+    // slice c / FS of the row: column group g = (c / 4) % 8, h = (c / 32) % H
+    uint8_t* base = row + (FS * 5 / 2) * (c / FS);
+    const uint32_t g = (c >> 2) & 7, h = (c >> 5) & (H - 1);
     *reinterpret_cast<uint2*>(base + 128 * (h >> 1) + 16 * g + 8 * (h & 1)) =
         make_uint2((r0 >> 16) | (r1 & 0xFFFF0000u), (r2 >> 16) | (r3 & 0xFFFF0000u));
-    *reinterpret_cast<uint16_t*>(base + 256 + 8 * g + 2 * h) =
+    *reinterpret_cast<uint16_t*>(base + 2 * FS + 2 * H * g + 2 * h) =
         uint16_t(((r0 >> 8) & 0xF0u) | ((r1 >> 12) & 0x0Fu) | (((r2 >> 8) & 0xF0u) << 8) |
                  (((r3 >> 12) & 0x0Fu) << 8));
 }
@@ -237,13 +242,17 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
 
         BitDecode dec;
         dec.init(g, tq);
-        // a row's slice f0 / 128 is 320 bytes at 320 (f0 / 128): this lane's
-        // halfwords of column groups h = 2hp, 2hp + 1 at 128 hp + 16 g, its 8
-        // nibble bytes at 256 + 8g
-        const uint8_t* Pl = a.bp + 320 * (blk.f0 / 128) + 16 * g;
-        const int nb_off = 256 - 8 * g;
+        // a row's slice f0 / FS is SB = 5 FS / 2 bytes at SB (f0 / FS): this
+        // lane's halfwords of column groups h = 2hp, 2hp + 1 at 128 hp + 16 g,
+        // its FS / 16 nibble bytes at 2 FS + (FS / 16) g
+        constexpr int SB = FS * 5 / 2;
+        const uint8_t* Pl = a.bp + SB * (blk.f0 / FS) + 16 * g;
+        const int nb_off = 2 * FS + (FS / 16) * g - 16 * g;
         float av0[U], av1[U];
-        uint2 h0[U][H], h1[U][H], n0[U], n1[U];
+        // nibble bytes per row: 8 at 128-column slices, 4 at 64
+        using Nib = std::conditional_t<H == 4, uint2, uint32_t>;
+        uint2 h0[U][H], h1[U][H];
+        Nib n0[U], n1[U];
         auto issue = [&](int u) {
             const uint32_t i0 = __shfl_sync(0xffffffffu, ma[(8 * u) / 32], (8 * u + tq) & 31);
             const uint32_t i1 = __shfl_sync(0xffffffffu, ma[(8 * u) / 32], (8 * u + tq + 4) & 31);
@@ -266,15 +275,21 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
                 h0[u][2 * hp + 1] = make_uint2(p0.z, p0.w);
                 h1[u][2 * hp + 1] = make_uint2(p1.z, p1.w);
             }
-            // nibbles of all 16 values in one load
-            n0[u] = ldg_u2_ordered(w0 + nb_off);
-            n1[u] = ldg_u2_ordered(w1 + nb_off);
+            // nibbles of all 4H values in one load
+            if constexpr (H == 4) {
+                n0[u] = ldg_u2_ordered(w0 + nb_off);
+                n1[u] = ldg_u2_ordered(w1 + nb_off);
+            } else {
+                n0[u] = ldg_u32_ordered(w0 + nb_off);
+                n1[u] = ldg_u32_ordered(w1 + nb_off);
+            }
         };
         // PF: lane 8U + e holds sparseA2B entry e of the group after the one
         // that load_meta fetched for issue, two groups ahead of the loads
         static_assert(!PF || (MA == 1 && 16 * U <= 32), "one prefetched row per lane");
         auto prefetch_rows = [&]() {
             if (PF && lane >= 8 * U && ma[0] < a.cols) {
+                static_assert(!PF || FS == 128, "the prefetch covers 320-byte slices");
                 const uint8_t* r = a.bp + size_t(ma[0]) * a.bpitch + 320 * (blk.f0 / 128);
                 if (PFK == 1) {
                     asm volatile("cp.async.bulk.prefetch.L2.global [%0], 320;" ::"l"(r) : "memory");
@@ -302,7 +317,11 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
                         while (blk.s_rwo[wl + 1] <= tt) ++wl;
                         next_bound = blk.s_rwo[wl + 1];
                     }
-                    tile_mma_packed<H>(acc, h0[u], n0[u], h1[u], n1[u], av0[u], av1[u]);
+                    if constexpr (H == 4)
+                        tile_mma_packed<H>(acc, h0[u], n0[u], h1[u], n1[u], av0[u], av1[u]);
+                    else
+                        tile_mma_packed<H>(acc, h0[u], make_uint2(n0[u], 0u), h1[u], make_uint2(n1[u], 0u),
+                                           av0[u], av1[u]);
                 }
                 issue(u);  // tile t + U + u
                 if (u == 0) prefetch_rows();  // tiles t + 2U .. t + 3U - 1

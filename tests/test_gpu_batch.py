@@ -109,13 +109,14 @@ def test_batch_rejects_bad_items():
 
 
 def test_batch_with_packed_b_matches_plain_bitwise():
-    """Wide TF32 items whose B the plan packs (all of them with
-    ACCSPMM_OPT_PACK = 1, small ones included) run in their own persistent
-    launch over packed copies the plan owns, packed again on every run: the
+    """TF32 items whose B the plan packs (all with K > 32 under
+    ACCSPMM_OPT_PACK = 1, small ones included; 128-column slices for K > 64,
+    64-column ones for K = 40, 64) run in their own persistent launches over
+    packed copies the plan owns, packed again on every run: the
     results equal one plain launch per matrix bit for bit, also from a graph
     replay after B has changed."""
     with capi.option(capi.OPT_PACK, 1):
-        items = build_items((128, 200, 64))
+        items = build_items((128, 200, 64, 40))
         ref = plain_results(items, capi.PREC_TF32)
         b = api.Batch(items)
         s = torch.cuda.Stream()

@@ -681,11 +681,13 @@ def test_packed_b_is_bit_identical(K):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("K", [72, 128, 200])
+@pytest.mark.parametrize("K", [40, 64, 72, 128, 200])
 def test_forced_packing_on_a_small_b_is_bit_identical(K):
     """ACCSPMM_OPT_PACK = 1 packs B wherever the launch shape allows, also below the
-    default rule's 4 MiB: ragged last slices (K = 72, 200), rows that are
-    not a multiple of the window height, the plain and adaptive entry points."""
+    default rule's 4 MiB, in 128-column slices (K = 72, 128, 200) and in the
+    160-byte 64-column slices of the K <= 64 shape (K = 40, 64): ragged last
+    slices, rows that are not a multiple of the window height, the plain and
+    adaptive entry points."""
     n = 5003
     rp, ci, vals = synth.powerlaw_local(n=n, seed=7)
     csr = dict(rows=n, cols=n, nnz=len(ci), row_ptr=rp, col_idx=ci, data=vals)
