@@ -127,28 +127,31 @@ struct PackDesc {
 };
 
 // Packs every listed B (pack_tf32_put layout) and writes each zero row; one
-// float4 of B per thread and step, read once with a streaming load.
+// float4 of B per thread and step, read once with a streaming load.  The
+// grid walks the B one after another (each block strides through B j, then
+// B j + 1), so no thread searches for its matrix.
 __global__ void pack_tf32_batch_kernel(const PackDesc* __restrict__ d, uint32_t n, uint64_t total) {
+    (void)total;
     for (uint32_t j = blockIdx.x; j < n; j += gridDim.x) {
         uint8_t* zero_row = d[j].P + (d[j].n4 / (d[j].K / 4)) * d[j].pitch;
         for (uint32_t t = threadIdx.x; t < d[j].pitch / 8; t += blockDim.x)
             reinterpret_cast<uint2*>(zero_row)[t] = make_uint2(0u, 0u);
     }
-    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
-         i += uint64_t(gridDim.x) * blockDim.x) {
-        uint32_t lo = 0, hi = n;  // last desc with start <= i
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) / 2;
-            if (d[mid].start <= i) lo = mid;
-            else hi = mid;
-        }
-        const PackDesc& x = d[lo];
-        const uint64_t local = i - x.start;
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    // thread t's first index in B j continues where its strides through the
+    // previous B ended, so every thread's work stays within one pass of the
+    // grid over the concatenated float4s
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    for (uint32_t j = 0; j < n; ++j) {
+        const PackDesc x = d[j];
         const uint32_t k4 = x.K / 4;
-        const uint64_t row = local / k4;
-        const uint32_t c = uint32_t(local - row * k4) * 4;
-        if (x.fs == 64) pack_tf32_put<64>(x.P + row * x.pitch, c, __ldcs(x.B + local));
-        else pack_tf32_put<128>(x.P + row * x.pitch, c, __ldcs(x.B + local));
+        for (; i < x.start + x.n4; i += stride) {
+            const uint64_t local = i - x.start;
+            const uint64_t row = local / k4;
+            const uint32_t c = uint32_t(local - row * k4) * 4;
+            if (x.fs == 64) pack_tf32_put<64>(x.P + row * x.pitch, c, __ldcs(x.B + local));
+            else pack_tf32_put<128>(x.P + row * x.pitch, c, __ldcs(x.B + local));
+        }
     }
 }
 
