@@ -61,14 +61,14 @@ __global__ void __launch_bounds__(NW * 32, MINB) spmm_window_kernel(const SpmmAr
 // The register-direct kernel with the rolling ring reading B from its packed
 // TF32 rows (a.bp): bit-identical to spmm_window_kernel<FS, TF32, U,
 // MINB, false, NW, true>, with a quarter fewer gathered sectors.
-template <int FS, int U, int MINB, int NW = kNW, bool PF = false, int PFK = 2>
+template <int FS, int U, int MINB, int NW = kNW, bool PF = false, int PFK = 2, bool EPI = false>
 __global__ void __launch_bounds__(NW * 32, MINB) spmm_window_packed_kernel(const SpmmArgs a) {
     extern __shared__ __align__(16) float smem[];
     float* part = smem;  // [2 * NW] slots
     uint32_t* s_rwo = reinterpret_cast<uint32_t*>(smem + 2 * NW * 8 * FS);
     Block<FS, NW> blk;
     blk.init(a, s_rwo, part);
-    direct_item_packed<FS, U, NW, PF, PFK>(a, blk);
+    direct_item_packed<FS, U, NW, PF, PFK, EPI>(a, blk);
 }
 
 // B rounded to TF32 (cvt.rna, as the SpMM's operands are) and packed row by
@@ -596,21 +596,21 @@ int launch_direct(const SpmmArgs& a, int occ, int ring, cudaStream_t s) {
     return epi ? launch_direct_t<FS, PREC, U, 2, true>(a, s) : launch_direct_t<FS, PREC, U, 2, false>(a, s);
 }
 
-template <int FS, int U, int MINB, bool PF = false, int PFK = 2>
+template <int FS, int U, int MINB, bool PF = false, int PFK = 2, bool EPI = false>
 int launch_packed_t(const SpmmArgs& a, cudaStream_t s) {
     const size_t smem = size_t(2 * kNW * 8 * FS) * 4 + size_t(a.wb + 1) * 4;
     static unsigned attr_set = 0;  // one bit per device
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 32 && !(attr_set & (1u << dev))) {
-        ACC_CUDA(cudaFuncSetAttribute(spmm_window_packed_kernel<FS, U, MINB, kNW, PF, PFK>,
+        ACC_CUDA(cudaFuncSetAttribute(spmm_window_packed_kernel<FS, U, MINB, kNW, PF, PFK, EPI>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
         attr_set |= 1u << dev;
     }
     const uint64_t grid = uint64_t(a.n_wblocks) * a.n_slices;
     if (grid == 0) return ACCSPMM_SUCCESS;
     if (grid > 0x7FFFFFFFull) ACC_FAIL(ACCSPMM_ERROR_OVERFLOW, "grid too large");
-    spmm_window_packed_kernel<FS, U, MINB, kNW, PF, PFK><<<unsigned(grid), kNW * 32, smem, s>>>(a);
+    spmm_window_packed_kernel<FS, U, MINB, kNW, PF, PFK, EPI><<<unsigned(grid), kNW * 32, smem, s>>>(a);
     ACC_LAUNCH_CHECK();
     return ACCSPMM_SUCCESS;
 }
@@ -667,13 +667,18 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     // in the same order
     Config cfg = choose_config(w_cfg, T, K, precision);
     // The bias/activation epilogue lengthens the store path inside the tile
-    // loop; at 128-column slices that made the register-direct kernel spill
-    // (2.76 ms against 2.31 ms without the epilogue on the 1M-row matrix at
-    // K = 128), so epilogue launches use 64-column slices at 3 CTAs per SM,
-    // which keep the ring without spilling (2.56 ms, against 2.78 ms for the
-    // SpMM followed by a separate bias + ReLU pass).  Same blocks, same
-    // arithmetic.
-    if ((epi.bias || epi.act) && !slice_fs && cfg.fs == 128) slice_fs = 64;
+    // loop; at 128-column slices that made the register-direct kernel reading
+    // fp32 B spill (2.76 ms against 2.31 ms without the epilogue on the
+    // 1M-row matrix at K = 128), so epilogue launches that do not pack B use
+    // 64-column slices at 3 CTAs per SM, which keep the ring without spilling
+    // (2.56 ms, against 2.78 ms for the SpMM followed by a separate bias +
+    // ReLU pass).  The packed-B kernel keeps its 128 registers without spills
+    // with the epilogue, so launches that pack B keep 128-column slices.
+    // Same blocks, same arithmetic.
+    const bool packs_at_128 = allow_pack && precision == ACCSPMM_PREC_TF32 && cfg.fs == 128 && cfg.occ == 2 &&
+                              cfg.ring != 0 &&
+                              (cfg.pack > 0 || (cfg.pack < 0 && uint64_t(cols) * K * 4 >= (uint64_t(4) << 20)));
+    if ((epi.bias || epi.act) && !slice_fs && cfg.fs == 128 && !packs_at_128) slice_fs = 64;
     if (slice_fs && slice_fs != cfg.fs) {
         // another slice width (the feature columns a CTA covers do not change
         // any element's arithmetic; the window blocks stay the chooser's)
@@ -759,7 +764,8 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     // 1.07 against 1.08 ms on 1M rows but 30.2 against 28.0 us on 16K rows
     const bool narrow_pack = cfg.fs == 64 && occ == 3 &&
                              (cfg.pack > 0 || (cfg.pack < 0 && K > 48 && K <= 64 && b_bytes >= (uint64_t(4) << 20)));
-    if (allow_pack && !x3 && !(epi.bias || epi.act) && ring_on && (wide_pack || narrow_pack)) {
+    const bool epi_on = epi.bias || epi.act;
+    if (allow_pack && !x3 && ring_on && (wide_pack || narrow_pack)) {
         cudaMemPool_t pool;
         int st = library_pool(&pool);
         if (st) return st;
@@ -790,7 +796,10 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
         if (st == ACCSPMM_SUCCESS && fs == 64) {
             // two tiles in flight per warp at 3 CTAs per SM, the unpacked
             // 64-column default's shape
-            st = launch_packed_t<64, 2, 3>(a, s);
+            st = epi_on ? launch_packed_t<64, 2, 3, false, 2, true>(a, s) : launch_packed_t<64, 2, 3>(a, s);
+        } else if (st == ACCSPMM_SUCCESS && epi_on) {
+            st = pf ? launch_packed_t<128, DirectBatch<128>::U, 2, true, 2, true>(a, s)
+                    : launch_packed_t<128, DirectBatch<128>::U, 2, false, 2, true>(a, s);
         } else if (st == ACCSPMM_SUCCESS) {
 #ifdef ACCSPMM_LAB
             if (pf && lab_env("ACCSPMM_PFK", 2) == 1)
@@ -846,7 +855,7 @@ int spmm_bias_act_impl(const accspmm_metcf_t* m, const float* B, float* C, uint3
     return spmm_window_launch_slices(m->row_window_offset, m->tc_offset, m->tc_local_bit,
                                      m->sparse_a2b, m->data, m->num_windows, m->num_windows,
                                      m->num_tiles, m->cols, B, C, K, precision, 0, 0xFFFFFFFFu, epi,
-                                     as_stream(stream), 0, m->owned != 0);
+                                     as_stream(stream), 0, m->owned != 0, true);
 }
 
 namespace {

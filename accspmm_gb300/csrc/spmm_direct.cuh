@@ -204,7 +204,7 @@ __device__ __forceinline__ void pack_tf32_put(uint8_t* row, uint32_t c, float4 v
 // 320-byte slice per row (its address operand is uniform, so the lanes'
 // prefetches issue one after another), 2 three prefetch.global.L2 of the
 // slice's 128-byte lines per row, issued by the lanes together.
-template <int FS, int U, int NW = kDirectNW, bool PF = false, int PFK = 2>
+template <int FS, int U, int NW = kDirectNW, bool PF = false, int PFK = 2, bool EPI = false>
 __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Block<FS, NW>& blk) {
     constexpr int H = FS / 32;
     using L = Layout<H>;
@@ -310,7 +310,7 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
                 const uint32_t tt = t + u;
                 if (tt < te) {
                     if (tt >= next_bound) {
-                        blk.template flush<false>(a, acc, wl, tb, te, first_win);
+                        blk.template flush<EPI>(a, acc, wl, tb, te, first_win);
                         first_win = false;
 #pragma unroll
                         for (int m = 0; m < NM; ++m) acc[m][0] = acc[m][1] = acc[m][2] = acc[m][3] = 0.f;
@@ -328,10 +328,10 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
             }
             load_meta(t + 2 * U);
         }
-        blk.template flush<false>(a, acc, wl, tb, te, first_win);
+        blk.template flush<EPI>(a, acc, wl, tb, te, first_win);
     }
     __syncthreads();
-    blk.template finish<false>(a);
+    blk.template finish<EPI>(a);
 }
 
 }  // namespace accspmm

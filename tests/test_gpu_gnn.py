@@ -47,6 +47,28 @@ def test_fused_epilogue_equals_separate_bias_and_relu(name, K, act):
     assert torch.equal(got2, torch.clamp_min(plain, 0.0))
 
 
+@pytest.mark.parametrize("K", [64, 128, 200])
+def test_fused_epilogue_over_packed_b_equals_separate_bias_and_relu(K):
+    """A B of 4 MiB or more is packed for the fused epilogue too (128-column
+    slices for K > 64, 64-column ones for K = 64): still bit for bit the plain
+    SpMM followed by a separate FP32 bias add and ReLU."""
+    from accspmm_gb300 import synth
+    n = 20000
+    rp, ci, vals = synth.powerlaw_local(n=n, seed=11)
+    csr = dict(rows=n, cols=n, nnz=len(ci), row_ptr=rp, col_idx=ci, data=vals)
+    m = api.DeviceMETCF.from_csr(api.DeviceCSR.upload(csr))
+    rng = np.random.default_rng(K)
+    B = torch_dev(rng.uniform(-1, 1, (n, K)).astype(np.float32))
+    assert B.numel() * 4 >= 4 << 20
+    bias = torch_dev(rng.uniform(-1, 1, K).astype(np.float32))
+    plain = empty_dev(m.c_rows, K)
+    m.spmm(B, plain, K)
+    got = empty_dev(m.c_rows, K)
+    m.spmm_bias_act(B, got, K, bias, capi.ACT_RELU)
+    torch.cuda.synchronize()
+    assert torch.equal(got, torch.clamp_min(plain + bias, 0.0))
+
+
 @pytest.mark.parametrize("prec,tol", [(capi.PREC_TF32, TOL_TF32_VS_F64),
                                       (capi.PREC_3XTF32, TOL_3XTF32_VS_F64)])
 def test_gcn_layer_against_fp64(prec, tol):
