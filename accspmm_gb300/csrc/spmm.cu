@@ -764,8 +764,17 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
     // 1.07 against 1.08 ms on 1M rows but 30.2 against 28.0 us on 16K rows
     const bool narrow_pack = cfg.fs == 64 && occ == 3 &&
                              (cfg.pack > 0 || (cfg.pack < 0 && K > 48 && K <= 64 && b_bytes >= (uint64_t(4) << 20)));
+    // 32-column slices at 3 CTAs per SM (the default for K <= 32): 80-byte
+    // packed slices, by default with a B of at least 4 MiB: adaptive step,
+    // packing included, 1M-row power-law matrix 0.63 against 0.84 ms at
+    // K = 32 and 0.61 against 0.73 ms at K = 16; 262,144 rows 165 against
+    // 196 us (K = 32); 65,536 rows 54 against 62 us (K = 32) and 53.5
+    // against 55.7 us (K = 16, a 4 MiB B); a 2 MiB B (the 16,384-row matrix
+    // at K = 32) lost, 24.8 against 20.8 us
+    const bool tiny_pack = cfg.fs == 32 && occ == 3 &&
+                           (cfg.pack > 0 || (cfg.pack < 0 && b_bytes >= (uint64_t(4) << 20)));
     const bool epi_on = epi.bias || epi.act;
-    if (allow_pack && !x3 && ring_on && (wide_pack || narrow_pack)) {
+    if (allow_pack && !x3 && ring_on && (wide_pack || narrow_pack || tiny_pack)) {
         cudaMemPool_t pool;
         int st = library_pool(&pool);
         if (st) return st;
@@ -778,7 +787,10 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
         const size_t n4 = size_t(cols) * (K / 4);
         const unsigned blocks = unsigned(std::min<size_t>((n4 + 255) / 256 + 1, size_t(sm_count()) * 16));
         // the packed rows, then the zero row at index cols that padding reads
-        if (fs == 64)
+        if (fs == 32)
+            pack_tf32_kernel<32><<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(B), static_cast<uint8_t*>(packed),
+                                                        K, pitch, n4, static_cast<uint8_t*>(packed) + size_t(cols) * pitch);
+        else if (fs == 64)
             pack_tf32_kernel<64><<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(B), static_cast<uint8_t*>(packed),
                                                         K, pitch, n4, static_cast<uint8_t*>(packed) + size_t(cols) * pitch);
         else
@@ -793,7 +805,9 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
         // 3.31 against 3.24 at K = 192 and 6.71 against 6.57 at K = 512
         const int pf_opt = option(ACCSPMM_OPT_PREFETCH);
         const bool pf = pf_opt == 1 || (pf_opt < 0 && (a.n_slices & 1u));
-        if (st == ACCSPMM_SUCCESS && fs == 64) {
+        if (st == ACCSPMM_SUCCESS && fs == 32) {
+            st = epi_on ? launch_packed_t<32, 4, 3, false, 2, true>(a, s) : launch_packed_t<32, 4, 3>(a, s);
+        } else if (st == ACCSPMM_SUCCESS && fs == 64) {
             // two tiles in flight per warp at 3 CTAs per SM, the unpacked
             // 64-column default's shape
             st = epi_on ? launch_packed_t<64, 2, 3, false, 2, true>(a, s) : launch_packed_t<64, 2, 3>(a, s);
@@ -986,7 +1000,7 @@ int spmm_adaptive_impl(const accspmm_adpbme_t* ad, const float* B, float* C, uin
 // the process exits.  All calls share the array, so calls that overlap on the
 // GPU (different streams, no ordering between them) race on it.  It never
 // packs B (that copy would need a scratch the size of B), so on a B of
-// 4 MiB or more at K > 48 it runs the kernel that reads fp32 B: the same
+// 4 MiB or more at K <= 32 or K > 48 it runs the kernel that reads fp32 B: the same
 // bits, 2.29 against 1.64 ms on the 1M-row power-law matrix at K = 128.
 // ---------------------------------------------------------------------------
 constexpr uint32_t kNoAllocWords = 1u << 20;  // 4 MiB: windows + 2 words
@@ -1067,7 +1081,10 @@ int autotune_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K
     for (const auto& ko : shapes)
         for (int fs : {32, 64, 128}) {
             if (fs > 32 && uint32_t(fs / 2) >= K) continue;  // slices far wider than K
-            for (uint32_t wb : {4u, 8u, 16u, 32u}) {
+            for (uint32_t wb : {1u, 2u, 4u, 8u, 16u, 32u}) {
+                // 1 and 2 windows per CTA only where the chooser itself goes
+                // below 4 (matrices of a few thousand windows)
+                if (wb < 4 && dflt.wb >= 4) continue;
                 Config c = dflt;
                 c.kernel = ko[0];
                 c.occ = ko[1];
@@ -1077,10 +1094,10 @@ int autotune_impl(const accspmm_metcf_t* m, const float* B, float* C, uint32_t K
                 c.slice_major = 0;
                 c.pack = 0;
                 cand.push_back(c);
-                // TF32 with the ring at 128-column slices (2 CTAs per SM) or 64 (3):
-                // also gathering from a packed B
+                // TF32 with the ring at 128-column slices (2 CTAs per SM), 64
+                // or 32 (3): also gathering from a packed B
                 if (precision == ACCSPMM_PREC_TF32 && c.kernel == kDirect && c.ring == 1 &&
-                    ((fs == 128 && c.occ == 2) || (fs == 64 && c.occ == 3))) {
+                    ((fs == 128 && c.occ == 2) || (fs <= 64 && c.occ == 3))) {
                     c.pack = 1;
                     cand.push_back(c);
                 }

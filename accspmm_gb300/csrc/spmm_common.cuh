@@ -107,6 +107,12 @@ __device__ __forceinline__ uint2 ldg_u2_ordered(const uint8_t* p) {
     return v;
 }
 
+__device__ __forceinline__ uint32_t ldg_u16_ordered(const uint8_t* p) {
+    unsigned short v;
+    asm volatile("ld.global.nc.u16 %0, [%1];" : "=h"(v) : "l"(p));
+    return v;
+}
+
 __device__ __forceinline__ uint32_t ldg_u32_ordered(const uint8_t* p) {
     uint32_t v;
     asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(v) : "l"(p));
@@ -213,11 +219,19 @@ __device__ __forceinline__ void tile_mma(float (&acc)[Layout<H>::NM][4], const f
 template <int H>
 __device__ __forceinline__ void tile_mma_packed(float (&acc)[Layout<H>::NM][4], const uint2 (&h0)[H], uint2 n0,
                                                 const uint2 (&h1)[H], uint2 n1, float av0, float av1) {
-    static_assert(H == 4 || H == 2, "packed B is gathered at 128- or 64-column slices");
+    static_assert(H == 4 || H == 2 || H == 1, "packed B is gathered at 128-, 64- or 32-column slices");
     constexpr int NM = Layout<H>::NM;
     const uint32_t b0 = f2tf32(av0), b1 = f2tf32(av1);
     const uint32_t n0s[2] = {n0.x << 4, n0.y << 4}, n1s[2] = {n1.x << 4, n1.y << 4};
     const uint32_t n0w[2] = {n0.x, n0.y}, n1w[2] = {n1.x, n1.y};
+    if constexpr (H == 1) {
+        // Layout<1>: MMA m takes values m and m + 2 of the lane's group
+        mma_tf32(acc[0], unpack_tf32<0, 0>(h0[0], n0w[0], n0s[0]), unpack_tf32<2, 0>(h0[0], n0w[0], n0s[0]),
+                 unpack_tf32<0, 0>(h1[0], n1w[0], n1s[0]), unpack_tf32<2, 0>(h1[0], n1w[0], n1s[0]), b0, b1);
+        mma_tf32(acc[1], unpack_tf32<1, 0>(h0[0], n0w[0], n0s[0]), unpack_tf32<3, 0>(h0[0], n0w[0], n0s[0]),
+                 unpack_tf32<1, 0>(h1[0], n1w[0], n1s[0]), unpack_tf32<3, 0>(h1[0], n1w[0], n1s[0]), b0, b1);
+        return;
+    }
 #pragma unroll
     for (int m = 0; m < NM; ++m) {
         const int hp = m >> 2, j = m & 3;

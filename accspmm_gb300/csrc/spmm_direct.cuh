@@ -181,19 +181,21 @@ __device__ __forceinline__ void direct_item(const SpmmArgs& a, const Block<FS, N
 // One float4 of B (columns c .. c + 3 of a row, c % 4 == 0) rounded to TF32
 // and stored into the row's packed form at `row`, the layout
 // direct_item_packed reads.  A row is cut into FS-column slices of
-// FS * 5 / 2 bytes (320 at FS = 128, 160 at FS = 64): the halfwords of bits
-// 31..16 of the slice's values (2 FS bytes), ordered so that each lane's
-// values come in runs of 16 bytes, then the nibbles of bits 15..12 (FS / 2
-// bytes, FS / 16 per lane).
+// FS * 5 / 2 bytes (320 at FS = 128, 160 at FS = 64, 80 at FS = 32): the
+// halfwords of bits 31..16 of the slice's values (2 FS bytes), ordered so
+// that each lane's values come in runs of 16 bytes (8 at FS = 32), then the
+// nibbles of bits 15..12 (FS / 2 bytes, FS / 16 per lane).
 template <int FS = 128>
 __device__ __forceinline__ void pack_tf32_put(uint8_t* row, uint32_t c, float4 v) {
-    static_assert(FS == 128 || FS == 64, "packed slices are 128 or 64 columns");
+    static_assert(FS == 128 || FS == 64 || FS == 32, "packed slices are 128, 64 or 32 columns");
     constexpr uint32_t H = FS / 32;
     const uint32_t r0 = f2tf32(v.x), r1 = f2tf32(v.y), r2 = f2tf32(v.z), r3 = f2tf32(v.w);
     // slice c / FS of the row: column group g = (c / 4) % 8, h = (c / 32) % H
     uint8_t* base = row + (FS * 5 / 2) * (c / FS);
     const uint32_t g = (c >> 2) & 7, h = (c >> 5) & (H - 1);
-    *reinterpret_cast<uint2*>(base + 128 * (h >> 1) + 16 * g + 8 * (h & 1)) =
+    // 32-column slices: one group per lane, halfwords in 8-byte runs
+    const uint32_t hw_off = FS == 32 ? 8 * g : 128 * (h >> 1) + 16 * g + 8 * (h & 1);
+    *reinterpret_cast<uint2*>(base + hw_off) =
         make_uint2((r0 >> 16) | (r1 & 0xFFFF0000u), (r2 >> 16) | (r3 & 0xFFFF0000u));
     *reinterpret_cast<uint16_t*>(base + 2 * FS + 2 * H * g + 2 * h) =
         uint16_t(((r0 >> 8) & 0xF0u) | ((r1 >> 12) & 0x0Fu) | (((r2 >> 8) & 0xF0u) << 8) |
@@ -246,10 +248,11 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
         // lane's halfwords of column groups h = 2hp, 2hp + 1 at 128 hp + 16 g,
         // its FS / 16 nibble bytes at 2 FS + (FS / 16) g
         constexpr int SB = FS * 5 / 2;
-        const uint8_t* Pl = a.bp + SB * (blk.f0 / FS) + 16 * g;
-        const int nb_off = 2 * FS + (FS / 16) * g - 16 * g;
+        constexpr int HW_LANE = FS == 32 ? 8 : 16;  // bytes between lanes' halfword runs
+        const uint8_t* Pl = a.bp + SB * (blk.f0 / FS) + HW_LANE * g;
+        const int nb_off = 2 * FS + (FS / 16) * g - HW_LANE * g;
         float av0[U], av1[U];
-        // nibble bytes per row: 8 at 128-column slices, 4 at 64
+        // nibble bytes per row: 8 at 128-column slices, 4 at 64, 2 at 32
         using Nib = std::conditional_t<H == 4, uint2, uint32_t>;
         uint2 h0[U][H], h1[U][H];
         Nib n0[U], n1[U];
@@ -275,10 +278,18 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
                 h0[u][2 * hp + 1] = make_uint2(p0.z, p0.w);
                 h1[u][2 * hp + 1] = make_uint2(p1.z, p1.w);
             }
+            if constexpr (H == 1) {
+                // the 4 values' halfwords, 8 bytes
+                h0[u][0] = ldg_u2_ordered(w0);
+                h1[u][0] = ldg_u2_ordered(w1);
+            }
             // nibbles of all 4H values in one load
             if constexpr (H == 4) {
                 n0[u] = ldg_u2_ordered(w0 + nb_off);
                 n1[u] = ldg_u2_ordered(w1 + nb_off);
+            } else if constexpr (H == 1) {
+                n0[u] = ldg_u16_ordered(w0 + nb_off);
+                n1[u] = ldg_u16_ordered(w1 + nb_off);
             } else {
                 n0[u] = ldg_u32_ordered(w0 + nb_off);
                 n1[u] = ldg_u32_ordered(w1 + nb_off);

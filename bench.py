@@ -195,7 +195,7 @@ def peaks():
 # the reason).
 KERNEL_SOURCES = ("accspmm_gb300/csrc/spmm.cu", "accspmm_gb300/csrc/spmm_direct.cuh",
                   "accspmm_gb300/csrc/spmm_common.cuh")
-TRAFFIC = {128: {"bytes": 8052707328, "src_sha": "1f9667aa55b82db7",
+TRAFFIC = {128: {"bytes": 8051597568, "src_sha": "910bbd0db6250c29",
                  "capture": "profiles/spmm_window_packed_kernel_powerlaw_local.md"}}
 
 
@@ -287,10 +287,10 @@ def cpu_baseline(rp, ci, v, B, budget_s=8.0):
 
 def launches_per_step_for(K, cols, prec, tune):
     """Kernels one SpMM call launches: the SpMM, preceded for TF32 with
-    K > 48 and a B of at least 4 MiB (the library's default rule, or as the
-    tuned shape says) by the launch that packs B."""
+    K <= 32 or K > 48 and a B of at least 4 MiB (the library's default rule,
+    or as the tuned shape says) by the launch that packs B."""
     from accspmm_gb300 import capi
-    pack = K > 48 and cols * K * 4 >= (4 << 20)
+    pack = (K <= 32 or K > 48) and cols * K * 4 >= (4 << 20)
     if tune is not None and tune["packed_b"] >= 0:
         pack = tune["packed_b"] == 1
     if os.environ.get("ACCSPMM_PACK", "") == "0":

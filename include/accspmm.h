@@ -243,12 +243,13 @@ void accspmm_adpbme_destroy(accspmm_adpbme_t* adp);
  * the blocks on the GPU, waits for that on the host once, and keeps the
  * schedule until accspmm_metcf_destroy (results do not depend on it).
  * Calls may be captured into a CUDA graph; a call captured before the
- * schedule exists runs the blocks in window order.  In TF32 with K > 48 and
- * a B of at least 4 MiB (or as a tuned shape says) a call first rounds B
- * to TF32 and packs each row to 2.5 bytes a value in a buffer of
- * 320 cols ceil(K / 128) bytes (160 cols at K <= 64) from the library's
- * memory pool (released in stream order): the SpMM then gathers 10 instead
- * of 16 sectors of each 128-column row slice (5 of 8 of a 64-column one),
+ * schedule exists runs the blocks in window order.  In TF32 with K <= 32 or
+ * K > 48 and a B of at least 4 MiB (or as a tuned shape says) a call first
+ * rounds B to TF32 and packs each row to 2.5 bytes a value in a buffer of
+ * 320 cols ceil(K / 128) bytes (160 cols at K <= 64, 80 cols at K <= 32)
+ * from the library's memory pool (released in stream order): the SpMM then
+ * gathers 10 instead of 16 sectors of each 128-column row slice (5 of 8 of
+ * a 64-column one, 3 of 4 of a 32-column one),
  * with bit-identical results, and at 128-column slices prefetches into L2
  * the rows of the tile group two ahead of the one it loads (when K spans an
  * odd number of 128-column slices).
@@ -371,7 +372,7 @@ int accspmm_spmm_host(const accspmm_metcf_t* metcf, const accspmm_adpbme_t* adp,
  * reported by accspmm_device_status, as for a caller-filled AdpBME there.
  * Unlike accspmm_spmm_adaptive it never packs B (the packed copy would need
  * 320 cols ceil(K / 128) bytes of scratch): on a B of 4 MiB or more at
- * K > 48 it runs the kernel that reads fp32 B, 2.29 against 1.64 ms per call
+ * K <= 32 or K > 48 it runs the kernel that reads fp32 B, 2.29 against 1.64 ms per call
  * on the 1M-row power-law matrix at K = 128 (GB300). */
 int accspmm_spmm_adaptive_noalloc(const accspmm_adpbme_t* adp, const float* B,
                                   float* C, uint32_t c_rows, uint32_t K,
@@ -447,9 +448,10 @@ void accspmm_autotune_clear(void);
  * kernel in a library built without them. */
 enum {
     ACCSPMM_OPT_PACK = 0,             /* ACCSPMM_PACK (0 -> 0, 2 -> 1): -1 (default) TF32
-                                         launches at 128-column slices (K > 64), and at
-                                         64-column slices with 48 < K <= 64, pack a B of at
-                                         least 4 MiB to 2.5-byte TF32 rows first; 0 never; 1
+                                         launches at 128-column slices (K > 64), at
+                                         64-column slices with 48 < K <= 64 and at 32-column
+                                         slices (K <= 32) pack a B of at least 4 MiB to
+                                         2.5-byte TF32 rows first; 0 never; 1
                                          whenever the launch shape allows */
     ACCSPMM_OPT_PREFETCH = 1,         /* ACCSPMM_PREFETCH (0 -> 0, 1 -> 1): -1 (default)
                                          the packed kernel prefetches into L2 the rows of

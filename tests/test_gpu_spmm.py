@@ -681,11 +681,12 @@ def test_packed_b_is_bit_identical(K):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("K", [40, 64, 72, 128, 200])
+@pytest.mark.parametrize("K", [16, 32, 40, 64, 72, 128, 200])
 def test_forced_packing_on_a_small_b_is_bit_identical(K):
     """ACCSPMM_OPT_PACK = 1 packs B wherever the launch shape allows, also below the
-    default rule's 4 MiB, in 128-column slices (K = 72, 128, 200) and in the
-    160-byte 64-column slices of the K <= 64 shape (K = 40, 64): ragged last
+    default rule's 4 MiB, in 128-column slices (K = 72, 128, 200), in the
+    160-byte 64-column slices of the K <= 64 shape (K = 40, 64) and in the
+    80-byte 32-column slices of the K <= 32 shape (K = 16, 32): ragged last
     slices, rows that are not a multiple of the window height, the plain and
     adaptive entry points."""
     n = 5003
