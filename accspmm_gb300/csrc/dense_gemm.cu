@@ -19,9 +19,10 @@
 // TF32 (dense_gemm_tf32_ws_kernel): persistent and warp-specialised -- copies,
 // rounding, MMAs into two alternating TMEM accumulators, and stores through
 // shared memory and tensor-map stores all overlap (described at the kernel).
-// 3xTF32 (dense_gemm_3xtf32_kernel): one tile per CTA; H and W are split into
-// hi + lo TF32 parts, three products per K step (hi*hi, hi*lo, lo*hi), and
-// every block's partial is summed in FP32 registers (described at the kernel).
+// 3xTF32 (dense_gemm_3xtf32_ws_kernel): the same structure; H and W are split
+// into hi + lo TF32 parts, three products per K step (hi*hi, hi*lo, lo*hi),
+// and every k-block's partial is summed in FP32 registers (described at the
+// kernel).
 //
 // Every wait is bounded (2 s of %globaltimer); a wait that runs out raises
 // a bit in the status word that accspmm_device_status reports, the CTA waits
@@ -47,7 +48,6 @@ __device__ unsigned int g_gemm_status = 0;
 
 constexpr int kBM = 128;       // rows of H per CTA: the MMA's M
 constexpr int kBK = 32;        // k per stage: one 128-byte swizzle row of fp32
-constexpr int kThreads = 128;  // four warps, one TMEM lane quarter each
 constexpr uint32_t kATileBytes = kBM * kBK * 4;  // 16 KB
 
 // Shared-memory matrix descriptor of a K-major operand tile written by a TMA
@@ -108,197 +108,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-struct GemmParams {
-    float* xw;        // n x k_out, row-major
-    uint32_t n, k_out;
-    uint32_t kblocks;  // ceil(k_in / 32)
-    uint32_t nt;       // output columns per CTA (multiple of 16; <= 256, 3xTF32 <= 128)
-    uint32_t stages;
-    uint32_t tmem_cols;  // power of two >= max(32, nt)
-    uint32_t stage_bytes;
-};
-
-// Shared memory of one 3xTF32 stage: [A hi 16 KB][A lo 16 KB][B hi nt*128][B lo nt*128],
-// every part 1024-byte aligned (nt is a multiple of 16, so nt * 128 is a multiple of 2048).
-__host__ __device__ constexpr uint32_t split_stage_bytes(uint32_t nt) { return 2u * (kATileBytes + nt * 128u); }
-
-// 3xTF32: one 128 x NT tile per CTA, every thread rounding and splitting
-// the H blocks, one thread issuing the MMAs (see the file's header).
-__global__ void __launch_bounds__(kThreads, 1)
-    dense_gemm_3xtf32_kernel(const __grid_constant__ CUtensorMap tm_h, const __grid_constant__ CUtensorMap tm_w,
-                      const __grid_constant__ CUtensorMap tm_wlo, const GemmParams p) {
-    extern __shared__ uint8_t dyn_smem[];
-    __shared__ __align__(8) uint64_t bars[2 * 8 + 3];  // full[8], empty[8], done, block done[2] (3xTF32)
-    __shared__ uint32_t s_tmem;
-    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t S = p.stages;
-    const uint32_t base = (smem_addr(dyn_smem) + 1023u) & ~1023u;
-    uint8_t* gbase = dyn_smem + (base - smem_addr(dyn_smem));
-    auto full = [&](uint32_t s) { return smem_addr(&bars[s]); };
-    auto empty = [&](uint32_t s) { return smem_addr(&bars[8 + s]); };
-    const uint32_t done = smem_addr(&bars[16]);
-    auto bdone = [&](uint32_t r) { return smem_addr(&bars[17 + r]); };
-    const uint32_t a_hi = 0, a_lo = kATileBytes, b_hi = 2u * kATileBytes, b_lo = b_hi + p.nt * 128u;
-    const uint32_t tx_bytes = kATileBytes + 2u * p.nt * 128u;
-
-    if (tid == 0) {
-        for (uint32_t s = 0; s < S; ++s) {
-            mbar_init(full(s), 1);
-            mbar_init(empty(s), 1);
-        }
-        mbar_init(done, 1);
-        mbar_init(bdone(0), 1);
-        mbar_init(bdone(1), 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&s_tmem)),
-                     "r"(p.tmem_cols)
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem = s_tmem;
-    const int m0 = int(blockIdx.x) * kBM;
-    const int n0 = int(blockIdx.y * p.nt);
-    const uint32_t idesc = idesc_tf32(kBM, p.nt);
-
-    uint32_t issued = 0;  // k-blocks whose copies were issued (thread 0)
-    bool stop = false;    // thread 0: a stage never came free, issue nothing more
-    auto issue = [&](uint32_t k) {
-        const uint32_t st = base + (k % S) * p.stage_bytes;
-        mbar_expect_tx(full(k % S), tx_bytes);
-        tma_load_2d(st + a_hi, &tm_h, int(k * kBK), m0, full(k % S));
-        tma_load_2d(st + b_hi, &tm_w, int(k * kBK), n0, full(k % S));
-        tma_load_2d(st + b_lo, &tm_wlo, int(k * kBK), n0, full(k % S));
-    };
-    if (tid == 0) {
-        for (; issued < S && issued < p.kblocks; ++issued) issue(issued);
-    }
-
-    // Each k-block's products go to their own tensor-memory region
-    // (block k to region k % 2: hi*hi in its first 128 columns, the two
-    // correction products in the next 128), and the block's partial is added
-    // to FP32 registers with round-to-nearest as soon as it is done; the
-    // tensor core accumulates only the four K = 8 steps of one block.  (One
-    // accumulator over all of k_in truncates at every step: 1.8e-6 relative
-    // error at k_in = 256, against about 2e-7 this way.)
-    float acc[128];
-#pragma unroll
-    for (int i = 0; i < 128; ++i) acc[i] = 0.f;
-    const uint32_t t_lane = (warp * 32u) << 16;
-    auto drain = [&](uint32_t b) -> bool {
-        const bool fin_b = __syncthreads_and(mbar_wait(bdone(b & 1u), (b >> 1) & 1u));
-        if (!fin_b) return false;
-        tc_fence_after();
-        const uint32_t t_main = tmem + t_lane + (b & 1u) * 256u;
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            if (uint32_t(c) * 16u < p.nt) {
-                float v[16], w[16];
-                tmem_ld16(t_main + c * 16, v);
-                tmem_ld16(t_main + 128 + c * 16, w);
-#pragma unroll
-                for (int i = 0; i < 16; ++i) acc[c * 16 + i] += v[i] + w[i];
-            }
-        }
-        tc_fence_before();
-        return true;
-    };
-
-    bool ok = true;
-    uint32_t k = 0;
-    for (; k < p.kblocks; ++k) {
-        const uint32_t s = k % S, ph = (k / S) & 1u;
-        const bool landed = mbar_wait(full(s), ph);
-        if (!__syncthreads_and(landed)) {
-            ok = false;
-            break;
-        }
-        // round the H tile to TF32 in place and keep the low part beside it
-        uint8_t* st = gbase + s * p.stage_bytes;
-        float4* ah = reinterpret_cast<float4*>(st + a_hi);
-        float4* al = reinterpret_cast<float4*>(st + a_lo);
-#pragma unroll
-        for (int i = 0; i < int(kATileBytes / 16 / kThreads); ++i) {
-            const uint32_t idx = tid + uint32_t(i) * kThreads;
-            float4 x = ah[idx];
-            float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
-            ah[idx] = h;
-            al[idx] = make_float4(tf32_hi(x.x - h.x), tf32_hi(x.y - h.y), tf32_hi(x.z - h.z),
-                                  tf32_hi(x.w - h.w));
-        }
-        // generic-proxy writes made visible to the tensor core's (async) reads
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            tc_fence_after();
-            const uint32_t sa = base + s * p.stage_bytes;
-#pragma unroll
-            for (uint32_t j = 0; j < kBK / 8; ++j) {
-                const uint64_t dah = kmajor_sw128_desc(sa + a_hi + j * 32);
-                const uint64_t dbh = kmajor_sw128_desc(sa + b_hi + j * 32);
-                const uint32_t t_main = tmem + (k & 1u) * 256u;
-                const uint64_t dal = kmajor_sw128_desc(sa + a_lo + j * 32);
-                const uint64_t dbl = kmajor_sw128_desc(sa + b_lo + j * 32);
-                umma_tf32(t_main, dah, dbh, idesc, j > 0 ? 1u : 0u);
-                umma_tf32(t_main + 128, dal, dbh, idesc, j > 0 ? 1u : 0u);
-                umma_tf32(t_main + 128, dah, dbl, idesc, 1u);
-            }
-            umma_commit(empty(s));
-            umma_commit(bdone(k & 1u));
-            if (!stop && issued < p.kblocks) {
-                // the stage is reused once the MMAs that read it are done
-                if (mbar_wait(empty(s), ph)) {
-                    issue(issued);
-                    ++issued;
-                } else {
-                    atomicOr(&g_gemm_status, 1u);
-                    stop = true;  // the wait for the block never issued fails for every thread
-                }
-            }
-        }
-        // the previous block's partial into the registers (its region is
-        // written again by block k + 1, after the next barrier)
-        if (k > 0 && !drain(k - 1)) {
-            ok = false;
-            break;
-        }
-    }
-    if (ok && p.kblocks > 0 && !drain(p.kblocks - 1)) ok = false;
-    if (tid == 0) {
-        if (!ok) {
-            atomicOr(&g_gemm_status, 1u);
-            // copies still in flight must land before the CTA exits
-            for (uint32_t j = k; j < issued; ++j) mbar_wait(full(j % S), (j / S) & 1u);
-        }
-        umma_commit(done);
-    }
-    const bool fin = __syncthreads_and(mbar_wait(done, 0));  // uniform: tcgen05.ld is warp-wide
-    if (!fin && tid == 0) atomicOr(&g_gemm_status, 1u);
-    tc_fence_after();
-    if (ok && fin) {
-        const int row = m0 + int(warp * 32 + lane);
-        if (row < int(p.n)) {
-            float* dst = p.xw + size_t(row) * p.k_out + n0;
-#pragma unroll
-            for (int q = 0; q < 32; ++q)
-                if (uint32_t(q) * 4u < p.nt && uint32_t(n0) + 4u * q < p.k_out)
-                    reinterpret_cast<float4*>(dst)[q] =
-                        make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
-        }
-    }
-    tc_fence_before();
-    __syncthreads();
-    if (warp == 0) {
-        tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(p.tmem_cols)
-                     : "memory");
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -552,6 +361,231 @@ __global__ void __launch_bounds__(kWsThreads, 1)
     }
 }
 
+// ---------------------------------------------------------------------------
+// 3xTF32, persistent and warp-specialised: the TF32 kernel's structure with
+// the operands split into hi + lo TF32 parts and a per-block drain of the
+// accumulators.  Fourteen warps:
+//   warp 0, one lane  -- copies: per k-block the 128 x 32 block of H and the
+//                        NT x 32 blocks of W^T hi and lo ("full");
+//   warps 2-5         -- split the H block in place: hi = rna(x) over x,
+//                        lo = rna(x - hi) beside it ("conv");
+//   warp 1, one lane  -- twelve MMAs per k-block into the region of its
+//                        parity: hi*hi into 128 columns, lo*hi and hi*lo into
+//                        the next 128 ("bfull"), freeing the stage ("empty");
+//   warps 6-13        -- two per TMEM lane quarter, each for 64 of the tile's
+//                        columns: add every block's main and correction
+//                        partials to FP32 registers with round-to-nearest as
+//                        soon as the block is done, free the region
+//                        ("bempty"), and after the item's last block store the
+//                        registers through shared memory and tensor-map
+//                        stores.
+// The tensor core accumulates only the four K = 8 steps of one block (its
+// own accumulation over all of k_in is not round-to-nearest and gave 1.8e-6
+// relative error at k_in = 256).
+
+constexpr int kX3Threads = 448;  // fourteen warps
+
+__global__ void __launch_bounds__(kX3Threads, 1)
+    dense_gemm_3xtf32_ws_kernel(const __grid_constant__ CUtensorMap tm_h, const __grid_constant__ CUtensorMap tm_w,
+                                const __grid_constant__ CUtensorMap tm_wlo, const __grid_constant__ CUtensorMap tm_out,
+                                const WsParams p) {
+    extern __shared__ uint8_t dyn_smem[];
+    // full[4], conv[4], empty[4], bfull[2], bempty[2], done
+    __shared__ __align__(8) uint64_t bars[3 * 4 + 5];
+    __shared__ uint32_t s_tmem;
+    __shared__ volatile int s_abort;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t S = p.stages;
+    const uint32_t base = (smem_addr(dyn_smem) + 1023u) & ~1023u;
+    uint8_t* gbase = dyn_smem + (base - smem_addr(dyn_smem));
+    const uint32_t out_base = base + S * p.stage_bytes;  // 8 drain warps x 4 KB
+    auto full = [&](uint32_t s) { return smem_addr(&bars[s]); };
+    auto conv = [&](uint32_t s) { return smem_addr(&bars[4 + s]); };
+    auto empty = [&](uint32_t s) { return smem_addr(&bars[8 + s]); };
+    auto bfull = [&](uint32_t r) { return smem_addr(&bars[12 + r]); };
+    auto bempty = [&](uint32_t r) { return smem_addr(&bars[14 + r]); };
+    const uint32_t done = smem_addr(&bars[16]);
+    // stage: [A hi 16 KB][A lo 16 KB][W^T hi nt x 128 B][W^T lo nt x 128 B]
+    const uint32_t a_lo = kATileBytes, b_hi = 2 * kATileBytes, b_lo = b_hi + p.nt * 128u;
+    const uint32_t tx_bytes = kATileBytes + 2u * p.nt * 128u;
+
+    if (tid == 0) {
+        for (uint32_t s = 0; s < S; ++s) {
+            mbar_init(full(s), 1);
+            mbar_init(conv(s), 4);
+            mbar_init(empty(s), 1);
+        }
+        for (uint32_t r = 0; r < 2; ++r) {
+            mbar_init(bfull(r), 1);
+            mbar_init(bempty(r), 8);
+        }
+        mbar_init(done, 1);
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&s_tmem)),
+                     "r"(512u)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = s_tmem;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            uint32_t it = 0;
+            bool go = true;
+            for (uint32_t item = blockIdx.x; go && item < p.items; item += gridDim.x) {
+                const int m0 = int(item / p.n_tiles) * kBM, n0 = int((item % p.n_tiles) * p.nt);
+                for (uint32_t kb = 0; kb < p.kblocks; ++kb, ++it) {
+                    const uint32_t s = it % S, use = it / S;
+                    if (use > 0 && !wait_or_abort(empty(s), (use - 1) & 1u, &s_abort)) {
+                        go = false;
+                        break;
+                    }
+                    const uint32_t st = base + s * p.stage_bytes;
+                    mbar_expect_tx(full(s), tx_bytes);
+                    tma_load_2d(st, &tm_h, int(kb * kBK), m0, full(s));
+                    tma_load_2d(st + b_hi, &tm_w, int(kb * kBK), n0, full(s));
+                    tma_load_2d(st + b_lo, &tm_wlo, int(kb * kBK), n0, full(s));
+                }
+            }
+            const uint32_t first = it > S ? it - S : 0;
+            for (uint32_t i = first; i < it; ++i) mbar_wait(full(i % S), (i / S) & 1u);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_tf32(kBM, p.nt);
+            uint32_t it = 0;  // k-blocks issued, over all items: block it uses region it & 1
+            bool go = true;
+            for (uint32_t item = blockIdx.x; go && item < p.items; item += gridDim.x) {
+                for (uint32_t kb = 0; kb < p.kblocks; ++kb, ++it) {
+                    const uint32_t s = it % S, r = it & 1u, use_r = it >> 1;
+                    if (use_r > 0 && !wait_or_abort(bempty(r), (use_r - 1) & 1u, &s_abort)) {
+                        go = false;
+                        break;
+                    }
+                    if (!wait_or_abort(conv(s), (it / S) & 1u, &s_abort)) {
+                        go = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t sa = base + s * p.stage_bytes;
+                    const uint32_t t_main = tmem + r * 256u;
+#pragma unroll
+                    for (uint32_t j = 0; j < kBK / 8; ++j) {
+                        const uint64_t dah = kmajor_sw128_desc(sa + j * 32);
+                        const uint64_t dal = kmajor_sw128_desc(sa + a_lo + j * 32);
+                        const uint64_t dbh = kmajor_sw128_desc(sa + b_hi + j * 32);
+                        const uint64_t dbl = kmajor_sw128_desc(sa + b_lo + j * 32);
+                        umma_tf32(t_main, dah, dbh, idesc, j > 0 ? 1u : 0u);
+                        umma_tf32(t_main + 128, dal, dbh, idesc, j > 0 ? 1u : 0u);
+                        umma_tf32(t_main + 128, dah, dbl, idesc, 1u);
+                    }
+                    umma_commit(empty(s));
+                    umma_commit(bfull(r));
+                }
+            }
+            umma_commit(done);
+            mbar_wait(done, 0);
+        }
+    } else if (warp < 6) {
+        // split: 128 threads, 8 float4 of each 16 KB H block
+        const uint32_t ct = tid - 64;
+        uint32_t it = 0;
+        bool go = true;
+        for (uint32_t item = blockIdx.x; go && item < p.items; item += gridDim.x) {
+            for (uint32_t kb = 0; kb < p.kblocks; ++kb, ++it) {
+                const uint32_t s = it % S;
+                if (!__all_sync(0xffffffffu, wait_or_abort(full(s), (it / S) & 1u, &s_abort))) {
+                    go = false;
+                    break;
+                }
+                float4* ah = reinterpret_cast<float4*>(gbase + s * p.stage_bytes);
+                float4* al = reinterpret_cast<float4*>(gbase + s * p.stage_bytes + a_lo);
+#pragma unroll
+                for (int i = 0; i < int(kATileBytes / 16 / 128); ++i) {
+                    const uint32_t idx = ct + uint32_t(i) * 128u;
+                    const float4 x = ah[idx];
+                    const float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
+                    ah[idx] = h;
+                    al[idx] = make_float4(tf32_hi(x.x - h.x), tf32_hi(x.y - h.y), tf32_hi(x.z - h.z),
+                                          tf32_hi(x.w - h.w));
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(conv(s));
+            }
+        }
+    } else {
+        // drain and store: TMEM lanes 32 (w % 4) .. +31, columns 64 hc .. +63
+        const uint32_t q = warp & 3u, hc = (warp - 6) >> 2;
+        const uint32_t obuf = out_base + (warp - 6) * kStageOut;
+        uint8_t* gobuf = gbase + (obuf - base);
+        const uint32_t t_lane = (q * 32u) << 16;
+        uint32_t it = 0;
+        bool go = true;
+        for (uint32_t item = blockIdx.x; go && item < p.items; item += gridDim.x) {
+            const int m0 = int(item / p.n_tiles) * kBM, n0 = int((item % p.n_tiles) * p.nt);
+            float acc[64];
+#pragma unroll
+            for (int i = 0; i < 64; ++i) acc[i] = 0.f;
+            for (uint32_t kb = 0; kb < p.kblocks; ++kb, ++it) {
+                const uint32_t r = it & 1u;
+                if (!__all_sync(0xffffffffu, wait_or_abort(bfull(r), (it >> 1) & 1u, &s_abort))) {
+                    go = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t t_main = tmem + r * 256u + t_lane + 64u * hc;
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    if (64u * hc + uint32_t(c) * 16u < p.nt) {
+                        float v[16], w[16];
+                        tmem_ld16(t_main + c * 16, v);
+                        tmem_ld16(t_main + 128 + c * 16, w);
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) acc[c * 16 + i] += v[i] + w[i];
+                    }
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bempty(r));
+            }
+            if (!go) break;
+            // the item's rows: two 32-column chunks through the staging buffer
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                const uint32_t col = 64u * hc + 32u * c;
+                if (col >= p.nt || uint32_t(m0) + q * 32u >= p.n || uint32_t(n0) + col >= p.k_out) continue;
+                // the previous store from this buffer has read it
+                if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                __syncwarp();
+                uint8_t* row = gobuf + lane * 128u;
+#pragma unroll
+                for (uint32_t j = 0; j < 8; ++j)
+                    *reinterpret_cast<float4*>(row + ((j ^ (lane & 7u)) * 16u)) =
+                        make_float4(acc[32 * c + 4 * j], acc[32 * c + 4 * j + 1], acc[32 * c + 4 * j + 2],
+                                    acc[32 * c + 4 * j + 3]);
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) tma_store_2d(&tm_out, n0 + int(col), m0 + int(q * 32), obuf);
+            }
+        }
+        if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        __syncwarp();
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512u) : "memory");
+    }
+}
+
 // W (k_in x k_out, row-major) to K-major W^T (k_out x kp, kp = k_in rounded
 // up to 4, zeros past k_in); in 3xTF32 also the split hi = rna(w), lo =
 // rna(w - hi) of every value.
@@ -610,38 +644,6 @@ int fp32_kmajor_map(EncodeTiledFn enc, CUtensorMap* tm, const float* base, uint6
     return ACCSPMM_SUCCESS;
 }
 
-int launch_gemm_3xtf32(const CUtensorMap& th, const CUtensorMap& tw, const CUtensorMap& twl, GemmParams p,
-                       cudaStream_t s) {
-    // stages: as many as fit in about 200 KB (at least two, at most eight and
-    // at most the number of k-blocks)
-    p.stage_bytes = split_stage_bytes(p.nt);
-    uint32_t st = (200u * 1024u) / p.stage_bytes;
-    st = st < 2 ? 2 : (st > 8 ? 8 : st);
-    if (st > p.kblocks) st = p.kblocks;
-    p.stages = st;
-    size_t smem = size_t(st) * p.stage_bytes + 1024;
-    // at most 512 / tmem_cols CTAs per SM, so that every CTA's tensor-memory
-    // allocation is granted at once: pad the shared memory (228 KB per SM)
-    const size_t cmax = 512 / p.tmem_cols;
-    const size_t smem_min = (228u * 1024u) / (cmax + 1) + 1;
-    if (smem < smem_min) smem = smem_min;
-    // dynamic shared memory, leaving room for the kernel's static barriers
-    constexpr size_t kMaxDyn = 226 * 1024;
-    if (smem > kMaxDyn) ACC_FAIL(ACCSPMM_ERROR_UNSUPPORTED, "shared memory %zu too large", smem);
-    static unsigned attr_set = 0;  // one bit per device
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev < 32 && !(attr_set & (1u << dev))) {
-        ACC_CUDA(cudaFuncSetAttribute(dense_gemm_3xtf32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      int(kMaxDyn)));
-        attr_set |= 1u << dev;
-    }
-    const dim3 grid((p.n + kBM - 1) / kBM, (p.k_out + p.nt - 1) / p.nt);
-    dense_gemm_3xtf32_kernel<<<grid, kThreads, smem, s>>>(th, tw, twl, p);
-    ACC_LAUNCH_CHECK();
-    return ACCSPMM_SUCCESS;
-}
-
 int launch_gemm_ws(const CUtensorMap& th, const CUtensorMap& tw, const CUtensorMap& tout, WsParams p,
                    cudaStream_t s) {
     constexpr size_t kMaxDyn = 226 * 1024;
@@ -663,6 +665,30 @@ int launch_gemm_ws(const CUtensorMap& th, const CUtensorMap& tw, const CUtensorM
     }
     const uint32_t grid = std::min<uint32_t>(p.items, uint32_t(sm_count()));
     dense_gemm_tf32_ws_kernel<<<grid, kWsThreads, smem, s>>>(th, tw, tout, p);
+    ACC_LAUNCH_CHECK();
+    return ACCSPMM_SUCCESS;
+}
+
+int launch_gemm_3xtf32_ws(const CUtensorMap& th, const CUtensorMap& tw, const CUtensorMap& twl,
+                          const CUtensorMap& tout, WsParams p, cudaStream_t s) {
+    constexpr size_t kMaxDyn = 226 * 1024;
+    const size_t fixed = 8 * kStageOut + 1024;  // store staging + alignment slack
+    p.stage_bytes = 2 * kATileBytes + 2 * p.nt * 128u;
+    uint32_t st = uint32_t((kMaxDyn - fixed) / p.stage_bytes);
+    p.stages = st > 4 ? 4 : st;
+    if (p.stages < 2) ACC_FAIL(ACCSPMM_ERROR_UNSUPPORTED, "shared memory too small for two stages");
+    size_t smem = size_t(p.stages) * p.stage_bytes + fixed;
+    if (smem < 115 * 1024) smem = 115 * 1024;  // one CTA per SM (it takes all 512 TMEM columns)
+    static unsigned attr_set = 0;  // one bit per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 32 && !(attr_set & (1u << dev))) {
+        ACC_CUDA(cudaFuncSetAttribute(dense_gemm_3xtf32_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      int(kMaxDyn)));
+        attr_set |= 1u << dev;
+    }
+    const uint32_t grid = std::min<uint32_t>(p.items, uint32_t(sm_count()));
+    dense_gemm_3xtf32_ws_kernel<<<grid, kX3Threads, smem, s>>>(th, tw, twl, tout, p);
     ACC_LAUNCH_CHECK();
     return ACCSPMM_SUCCESS;
 }
@@ -733,40 +759,27 @@ int dense_gemm_impl(const float* H, uint32_t n, uint32_t k_in, const float* W, u
             ACC_FAIL(ACCSPMM_ERROR_CUDA, "transpose launch failed: %s", cudaGetErrorString(le));
         }
     }
-    GemmParams p{};
-    p.xw = XW;
-    p.n = n;
-    p.k_out = k_out;
-    p.kblocks = (kp + kBK - 1) / kBK;
-    // TF32: up to 256 output columns per CTA, one accumulator; 3xTF32: up to
-    // 128, four 128-column regions (two blocks in flight, main and correction
-    // products each)
-    p.nt = std::min<uint32_t>(split ? 128 : 256, (k_out + 15) & ~15u);
-    p.tmem_cols = 32;
-    while (p.tmem_cols < p.nt) p.tmem_cols <<= 1;
-    if (split) p.tmem_cols = 512;
-    CUtensorMap th, tw, twl;
+    // TF32: up to 256 output columns per work item, two alternating TMEM
+    // accumulators; 3xTF32: up to 128, the four 128-column regions of two
+    // k-blocks in flight (main and correction products each)
+    WsParams w{};
+    w.n = n;
+    w.k_out = k_out;
+    w.kblocks = (kp + kBK - 1) / kBK;
+    w.nt = std::min<uint32_t>(split ? 128 : 256, (k_out + 15) & ~15u);
+    w.n_tiles = (k_out + w.nt - 1) / w.nt;
+    w.items = ((n + kBM - 1) / kBM) * w.n_tiles;  // below 2^32: n < 2^32, n_tiles <= 2^24 / 16
+    w.acc_stride = 32;
+    while (w.acc_stride < w.nt) w.acc_stride <<= 1;
+    w.tmem_cols = split ? 512 : 2 * w.acc_stride;
+    // XW written by tensor-map stores of 32 x 32 boxes (rows past n and
+    // columns past k_out are not written)
+    CUtensorMap th, tw, twl, tout;
     r = fp32_kmajor_map(enc, &th, h, n, kp, kBM);
-    if (!r) r = fp32_kmajor_map(enc, &tw, wt, k_out, kp, p.nt);
-    if (!r) r = fp32_kmajor_map(enc, &twl, split ? wt_lo : wt, k_out, kp, p.nt);
-    if (!r && split) r = launch_gemm_3xtf32(th, tw, twl, p, s);
-    if (!r && !split) {
-        // XW written by tensor-map stores of 32 x 32 boxes (rows past n and
-        // columns past k_out are not written)
-        CUtensorMap tout;
-        r = fp32_kmajor_map(enc, &tout, XW, n, k_out, 32);
-        WsParams w{};
-        w.n = n;
-        w.k_out = k_out;
-        w.kblocks = p.kblocks;
-        w.nt = p.nt;
-        w.n_tiles = (k_out + p.nt - 1) / p.nt;
-        w.items = ((n + kBM - 1) / kBM) * w.n_tiles;  // below 2^32: n < 2^32, n_tiles <= 2^24 / 16
-        w.acc_stride = 32;
-        while (w.acc_stride < p.nt) w.acc_stride <<= 1;
-        w.tmem_cols = 2 * w.acc_stride;
-        if (!r) r = launch_gemm_ws(th, tw, tout, w, s);
-    }
+    if (!r) r = fp32_kmajor_map(enc, &tw, wt, k_out, kp, w.nt);
+    if (!r) r = fp32_kmajor_map(enc, &twl, split ? wt_lo : wt, k_out, kp, w.nt);
+    if (!r) r = fp32_kmajor_map(enc, &tout, XW, n, k_out, 32);
+    if (!r) r = split ? launch_gemm_3xtf32_ws(th, tw, twl, tout, w, s) : launch_gemm_ws(th, tw, tout, w, s);
     give_back();
     return r;
 }
