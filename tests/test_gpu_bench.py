@@ -78,9 +78,25 @@ def test_reference_arm_gpu_kernels():
     assert d["value"] > 0 and d["impl"] == "reference"
 
 
+def test_both_arms_print_the_same_config():
+    """The reference arm and ours identify the workload with the same config
+    dict (sizes, realised degrees, tiles, windows, groups, seed), so that a
+    comparison of the two lines can check they measured the same thing."""
+    ours = run("--n", "65536", "--k", "64", "--steps", "2", "--warmup", "3", "--no-sweep",
+               "--no-host-build", "--no-autotune", "--no-extras", "--no-cpu-baseline", "--no-cusparse")
+    ref = run("--impl", "reference", "--n", "65536", "--k", "64", "--steps", "2", "--warmup", "1",
+              "--no-ref-gpu")
+    assert ours["config"] == ref["config"]
+    ours_s = run("--workload", "small", "--steps", "5", "--warmup", "3", "--no-cpu-baseline", "--no-autotune")
+    ref_s = run("--impl", "reference", "--workload", "small", "--steps", "2", "--warmup", "1", "--no-ref-gpu")
+    assert ours_s["config"] == ref_s["config"]
+
+
 def test_profile_modes_run():
     """The commands the ncu summaries were made with keep running."""
     d = run("--profile", "1", "--n", "65536", "--k", "64")
     assert d["profile_launches"] == 1 and d["tiles"] > 0
+    d = run("--profile-step", "2", "--n", "65536", "--k", "128", "--no-autotune")
+    assert d["profile_steps"] == 2 and d["path"] in ("plain", "adaptive")
     d = run("--workload", "small", "--profile", "2")
     assert d["profile_launches"] == 2
