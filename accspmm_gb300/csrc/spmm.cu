@@ -68,6 +68,10 @@ __global__ void __launch_bounds__(NW * 32, MINB) spmm_window_packed_kernel(const
     uint32_t* s_rwo = reinterpret_cast<uint32_t*>(smem + 2 * NW * 8 * FS);
     Block<FS, NW> blk;
     blk.init(a, s_rwo, part);
+    // launched as a programmatic dependent of the packing launch: the block
+    // set-up above overlaps its tail; the packed rows are read only after it
+    // has finished and its writes are visible
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     direct_item_packed<FS, U, NW, PF, PFK, EPI>(a, blk);
 }
 
@@ -85,6 +89,9 @@ __global__ void __launch_bounds__(NW * 32, MINB) spmm_window_packed_kernel(const
 template <int FS = 128>
 __global__ void pack_tf32_kernel(const float4* __restrict__ B, uint8_t* __restrict__ P, uint32_t K,
                                  uint32_t pitch, size_t n4, uint8_t* __restrict__ zero_row) {
+    // the SpMM launched after this one may start its set-up once every block
+    // of this grid has started
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const uint32_t k4 = K / 4;
     // the zero row read for padding columns (pitch is a multiple of 8)
     if (blockIdx.x == 0)
@@ -610,8 +617,19 @@ int launch_packed_t(const SpmmArgs& a, cudaStream_t s) {
     const uint64_t grid = uint64_t(a.n_wblocks) * a.n_slices;
     if (grid == 0) return ACCSPMM_SUCCESS;
     if (grid > 0x7FFFFFFFull) ACC_FAIL(ACCSPMM_ERROR_OVERFLOW, "grid too large");
-    spmm_window_packed_kernel<FS, U, MINB, kNW, PF, PFK, EPI><<<unsigned(grid), kNW * 32, smem, s>>>(a);
-    ACC_LAUNCH_CHECK();
+    // a programmatic dependent launch of the packing kernel before it (the
+    // kernel waits for it with griddepcontrol.wait before reading B)
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(unsigned(grid));
+    lc.blockDim = dim3(kNW * 32);
+    lc.dynamicSmemBytes = smem;
+    lc.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    ACC_CUDA(cudaLaunchKernelEx(&lc, spmm_window_packed_kernel<FS, U, MINB, kNW, PF, PFK, EPI>, a));
     return ACCSPMM_SUCCESS;
 }
 

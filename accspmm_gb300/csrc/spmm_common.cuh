@@ -230,8 +230,7 @@ __device__ __forceinline__ void tile_mma_packed(float (&acc)[Layout<H>::NM][4], 
                  unpack_tf32<0, 0>(h1[0], n1w[0], n1s[0]), unpack_tf32<2, 0>(h1[0], n1w[0], n1s[0]), b0, b1);
         mma_tf32(acc[1], unpack_tf32<1, 0>(h0[0], n0w[0], n0s[0]), unpack_tf32<3, 0>(h0[0], n0w[0], n0s[0]),
                  unpack_tf32<1, 0>(h1[0], n1w[0], n1s[0]), unpack_tf32<3, 0>(h1[0], n1w[0], n1s[0]), b0, b1);
-        return;
-    }
+    } else {
 #pragma unroll
     for (int m = 0; m < NM; ++m) {
         const int hp = m >> 2, j = m & 3;
@@ -246,6 +245,7 @@ __device__ __forceinline__ void tile_mma_packed(float (&acc)[Layout<H>::NM][4], 
         ACC_PK(0) ACC_PK(1) ACC_PK(2) ACC_PK(3)
 #undef ACC_PK
         mma_tf32(acc[m], x0, x1, x2, x3, b0, b1);
+    }
     }
 }
 
