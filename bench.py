@@ -109,34 +109,105 @@ def workload_name(n, k):
 
 
 class ClockSampler:
-    """nvidia-smi samples every 200 ms while the timed region runs."""
+    """SM clock and clock-event (throttle) reasons sampled while the timed
+    region runs: read in this process through NVML every millisecond (read
+    only), so that a timed region of a few tens of milliseconds still gets
+    tens of samples; where NVML cannot be loaded, nvidia-smi every 100 ms.
+    `index` is the CUDA device; NVML finds it by UUID (the CUDA index and
+    the NVML index differ when CUDA_VISIBLE_DEVICES is set)."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason* bits of nvml.h
+    REASON_BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20,
+                   "hw_thermal_slowdown": 0x40, "hw_power_brake_slowdown": 0x80}
+    PERIOD_S = 0.001
 
     def __init__(self, index: int):
         self.index = index
-        self.lines = []
+        self.samples = []  # (sm MHz, max sm MHz, {reason names})
         self.proc = None
+        self.nvml = None
+        self.stop = threading.Event()
+        self.source = None
+
+    def _nvml_open(self):
+        import ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            return None
+        h = ctypes.c_void_p()
+        found = False
+        try:
+            import torch
+            uuid = str(torch.cuda.get_device_properties(self.index).uuid)
+            found = lib.nvmlDeviceGetHandleByUUID(("GPU-" + uuid).encode(), ctypes.byref(h)) == 0
+        except Exception:
+            found = False
+        if not found and lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.index), ctypes.byref(h)) != 0:
+            lib.nvmlShutdown()
+            return None
+        get_reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        return lib, h, get_reasons
+
+    def _nvml_read(self):
+        import ctypes
+        lib, h, get_reasons = self.nvml
+        clk, mx, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        sm_clock = 1  # NVML_CLOCK_SM
+        while not self.stop.is_set():
+            if (lib.nvmlDeviceGetClockInfo(h, sm_clock, ctypes.byref(clk)) == 0 and
+                    lib.nvmlDeviceGetMaxClockInfo(h, sm_clock, ctypes.byref(mx)) == 0 and
+                    get_reasons(h, ctypes.byref(rs)) == 0):
+                self.samples.append((float(clk.value), float(mx.value),
+                                     {n for n, bit in self.REASON_BITS.items() if rs.value & bit}))
+            time.sleep(self.PERIOD_S)
 
     def __enter__(self):
+        try:
+            self.nvml = self._nvml_open()
+        except (OSError, AttributeError):
+            self.nvml = None
+        if self.nvml:
+            self.source = "nvml, 1 ms"
+            self.t = threading.Thread(target=self._nvml_read, daemon=True)
+            self.t.start()
+            # the first sample lands before the timed region starts
+            deadline = time.time() + 1.0
+            while not self.samples and time.time() < deadline:
+                time.sleep(self.PERIOD_S)
+            return self
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
                  "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
+            self.source = "nvidia-smi, 100 ms"
+            self.t = threading.Thread(target=self._smi_read, daemon=True)
             self.t.start()
         except OSError:
             self.proc = None
         return self
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
+    def _smi_read(self):
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.proc.stdout:
+            f = [x.strip() for x in ln.strip().split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm, mx = float(f[1]), float(f[2])
+            except ValueError:
+                continue
+            self.samples.append((sm, mx, {nm for nm, val in zip(names, f[5:9]) if val.lower() == "active"}))
 
     def __exit__(self, *exc):
+        if self.nvml:
+            self.stop.set()
+            self.t.join(timeout=5)
+            self.nvml[0].nvmlShutdown()
         if self.proc:
             self.proc.terminate()
             try:
@@ -145,24 +216,14 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            f = [x.strip() for x in ln.split(",")]
-            if len(f) < 9:
-                continue
-            try:
-                sm.append(float(f[1]))
-                mx.append(float(f[2]))
-            except ValueError:
-                continue
-            for nm, val in zip(names, f[5:9]):
-                if val.lower() == "active":
-                    reasons.add(nm)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
-                "reasons": sorted(reasons), "samples": len(sm)}
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0, "source": self.source}
+        reasons = set()
+        for _, _, r in self.samples:
+            reasons |= r
+        return {"sm_mhz": statistics.median(x[0] for x in self.samples),
+                "sm_max_mhz": max(x[1] for x in self.samples),
+                "reasons": sorted(reasons), "samples": len(self.samples), "source": self.source}
 
 
 def algorithmic_bytes(nnz, T, W, cols, K, G=None, c_rows=None):
@@ -195,7 +256,7 @@ def peaks():
 # the reason).
 KERNEL_SOURCES = ("accspmm_gb300/csrc/spmm.cu", "accspmm_gb300/csrc/spmm_direct.cuh",
                   "accspmm_gb300/csrc/spmm_common.cuh")
-TRAFFIC = {128: {"bytes": 8051597568, "src_sha": "910bbd0db6250c29",
+TRAFFIC = {128: {"bytes": 8053316101, "src_sha": "a721cfe246a37415",
                  "capture": "profiles/spmm_window_packed_kernel_powerlaw_local.md"}}
 
 
