@@ -155,13 +155,22 @@ __device__ __forceinline__ uint32_t adp_step(uint32_t st, uint32_t a, uint32_t t
     return *split ? a + 1 : tau + a + 1;
 }
 
-constexpr uint32_t kAdpChunk = 4096;
+// The greedy packing is a finite-state machine over the tiles: its input per
+// tile is whether the tile starts a window (cost a_first) or not (a_other).
+// Tiles are cut into chunks of kAdpChunk; each chunk tabulates the state it
+// ends in for every state it may start in, the tables are composed level by
+// level (kAdpGroup chunks into one table, then a walk over those), and every
+// chunk replays its tiles from its true start state to mark the splits.
+// Each step is exact integer arithmetic, so the marks equal a sequential walk.
+constexpr uint32_t kAdpChunk = 256;   // tiles per chunk (one warp replays one chunk)
+constexpr uint32_t kAdpPiece = 16384; // u16 table entries staged in shared memory at a time
 
 __device__ __forceinline__ bool is_first_tile(const uint32_t* row_indices, uint32_t t) {
     return t == 0 || row_indices[t] != row_indices[t - 1];
 }
 
-// table[c][s] = state after chunk c when entered in state s.
+// table[c][s] = state after chunk c when entered in state s (one block per
+// chunk, one thread per state).
 __global__ void adp_chunk_table_kernel(const uint32_t* __restrict__ row_indices, uint32_t T,
                                        uint32_t a_first, uint32_t a_other, uint32_t target,
                                        uint32_t nstates, uint16_t* __restrict__ table) {
@@ -179,27 +188,92 @@ __global__ void adp_chunk_table_kernel(const uint32_t* __restrict__ row_indices,
     }
 }
 
-__global__ void adp_chain_kernel(const uint16_t* __restrict__ table, uint32_t nchunks,
-                                 uint32_t nstates, uint32_t* __restrict__ in_state) {
-    uint32_t st = 0;
-    for (uint32_t c = 0; c < nchunks; ++c) {
-        in_state[c] = st;
-        st = table[size_t(c) * nstates + st];
+// out[b][s] = the composition of tables b*group .. min(n, (b+1)*group) - 1
+// applied to s (one block per group, one thread per state; the group's
+// tables are staged in shared memory, group * nstates <= kAdpPiece).
+__global__ void adp_compose_kernel(const uint16_t* __restrict__ table, uint32_t n, uint32_t nstates,
+                                   uint32_t group, uint16_t* __restrict__ out) {
+    __shared__ uint16_t tab[kAdpPiece];
+    const uint32_t c0 = blockIdx.x * group, cnt = min(group, n - c0);
+    const uint16_t* src = table + size_t(c0) * nstates;
+    for (uint32_t j = threadIdx.x; j < cnt * nstates; j += blockDim.x) tab[j] = src[j];
+    __syncthreads();
+    for (uint32_t s = threadIdx.x; s < nstates; s += blockDim.x) {
+        uint32_t st = s;
+        for (uint32_t j = 0; j < cnt; ++j) st = tab[j * nstates + st];
+        out[size_t(blockIdx.x) * nstates + s] = uint16_t(st);
     }
 }
 
+// Block b walks tables b*group .. min(n, (b+1)*group) - 1 from the state
+// start[b] (0 when start is null) and writes the state each table is
+// entered in: in_state[c].  The tables pass through shared memory in
+// pieces; one thread walks each piece.
+__global__ void adp_walk_kernel(const uint16_t* __restrict__ table, uint32_t n, uint32_t nstates,
+                                uint32_t group, const uint32_t* __restrict__ start,
+                                uint32_t* __restrict__ in_state) {
+    __shared__ uint16_t tab[kAdpPiece];
+    __shared__ uint32_t st_sh;
+    const uint32_t c0 = blockIdx.x * group, c1 = min(n, c0 + group);
+    const uint32_t per_piece = kAdpPiece / nstates;
+    if (threadIdx.x == 0) st_sh = start ? start[blockIdx.x] : 0u;
+    for (uint32_t p0 = c0; p0 < c1; p0 += per_piece) {
+        const uint32_t cnt = min(per_piece, c1 - p0);
+        const uint16_t* src = table + size_t(p0) * nstates;
+        __syncthreads();  // the previous piece is walked
+        for (uint32_t j = threadIdx.x; j < cnt * nstates; j += blockDim.x) tab[j] = src[j];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t st = st_sh;
+            for (uint32_t j = 0; j < cnt; ++j) {
+                in_state[p0 + j] = st;
+                st = tab[j * nstates + st];
+            }
+            st_sh = st;
+        }
+    }
+}
+
+// One warp per chunk: the chunk's window-start flags become eight ballot
+// words, one lane walks the 256 steps from the chunk's start state
+// collecting the split marks as bits, and the warp stores them as flags.
 __global__ void adp_replay_kernel(const uint32_t* __restrict__ row_indices, uint32_t T,
                                   uint32_t a_first, uint32_t a_other, uint32_t target,
                                   const uint32_t* __restrict__ in_state, uint32_t nchunks,
                                   uint32_t* __restrict__ split_flag) {
-    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    static_assert(kAdpChunk == 8 * 32, "eight ballot words per chunk");
+    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31;
     if (c >= nchunks) return;
+    const uint32_t t0 = c * kAdpChunk, len = min(kAdpChunk, T - t0);
+    uint32_t firsts[8], splits[8];
+    uint32_t prev = (lane == 0 && t0 > 0) ? row_indices[t0 - 1] : 0u;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const uint32_t i = j * 32 + lane;
+        const uint32_t r = i < len ? row_indices[t0 + i] : 0u;
+        const uint32_t up = __shfl_up_sync(0xffffffffu, r, 1);
+        const uint32_t before = lane == 0 ? prev : up;
+        const bool f = i < len && (t0 + i == 0 || r != before);
+        firsts[j] = __ballot_sync(0xffffffffu, f);
+        prev = __shfl_sync(0xffffffffu, r, 31);
+    }
     uint32_t st = in_state[c];
-    const uint32_t t0 = c * kAdpChunk, t1 = min(t0 + kAdpChunk, T);
-    for (uint32_t t = t0; t < t1; ++t) {
-        bool sp;
-        st = adp_step(st, is_first_tile(row_indices, t) ? a_first : a_other, target, &sp);
-        split_flag[t] = sp ? 1u : 0u;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        uint32_t bits = 0;
+        const uint32_t n_here = len > uint32_t(j) * 32 ? min(32u, len - uint32_t(j) * 32) : 0u;
+        for (uint32_t b = 0; b < n_here; ++b) {
+            bool sp;
+            st = adp_step(st, ((firsts[j] >> b) & 1u) ? a_first : a_other, target, &sp);
+            bits |= uint32_t(sp) << b;
+        }
+        splits[j] = bits;
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const uint32_t i = j * 32 + lane;
+        if (i < len) split_flag[t0 + i] = (splits[j] >> lane) & 1u;
     }
 }
 
@@ -400,16 +474,30 @@ int adpbme_from_metcf_device(const accspmm_metcf_t* m, uint32_t t_load, uint32_t
     const uint64_t nstates = smax + 2;
     if (T) {
         if (nstates <= 1024 && smax + 1 < 65535) {
+            const uint32_t ns = uint32_t(nstates);
             const uint32_t nch = (T + kAdpChunk - 1) / kAdpChunk;
-            ACC_CUDA(table.alloc(size_t(nch) * nstates, s));
+            // chunks per composed table: as many as fit one shared-memory piece
+            const uint32_t group = std::max<uint32_t>(1, std::min<uint32_t>(64, kAdpPiece / ns));
+            const uint32_t nsup = (nch + group - 1) / group;
+            DevBuf<uint16_t> sup;
+            DevBuf<uint32_t> sup_in;
+            ACC_CUDA(table.alloc(size_t(nch) * ns, s));
             ACC_CUDA(in_state.alloc(nch, s));
-            unsigned thr = unsigned(std::min<uint64_t>(1024, (nstates + 31) / 32 * 32));
-            adp_chunk_table_kernel<<<nch, thr, 0, s>>>(ri.p, T, af, ao, target, uint32_t(nstates), table.p);
+            ACC_CUDA(sup.alloc(size_t(nsup) * ns, s));
+            ACC_CUDA(sup_in.alloc(nsup, s));
+            const unsigned thr = unsigned(std::min<uint64_t>(1024, (nstates + 31) / 32 * 32));
+            adp_chunk_table_kernel<<<nch, thr, 0, s>>>(ri.p, T, af, ao, target, ns, table.p);
             ACC_LAUNCH_CHECK();
-            adp_chain_kernel<<<1, 1, 0, s>>>(table.p, nch, uint32_t(nstates), in_state.p);
+            adp_compose_kernel<<<nsup, thr, 0, s>>>(table.p, nch, ns, group, sup.p);
             ACC_LAUNCH_CHECK();
-            adp_replay_kernel<<<blocks_for(nch, 128), 128, 0, s>>>(ri.p, T, af, ao, target, in_state.p,
-                                                                   nch, flag.p);
+            // the composed tables in order from state 0, then each group's
+            // chunks from its composed start state
+            adp_walk_kernel<<<1, 256, 0, s>>>(sup.p, nsup, ns, nsup, nullptr, sup_in.p);
+            ACC_LAUNCH_CHECK();
+            adp_walk_kernel<<<nsup, 256, 0, s>>>(table.p, nch, ns, group, sup_in.p, in_state.p);
+            ACC_LAUNCH_CHECK();
+            adp_replay_kernel<<<blocks_for(size_t(nch) * 32, 256), 256, 0, s>>>(ri.p, T, af, ao, target,
+                                                                               in_state.p, nch, flag.p);
             ACC_LAUNCH_CHECK();
         } else {
             adp_sequential_kernel<<<1, 1, 0, s>>>(ri.p, T, af, ao, target, flag.p);
