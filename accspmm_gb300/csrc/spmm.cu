@@ -823,12 +823,18 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
         // 3.31 against 3.24 at K = 192 and 6.71 against 6.57 at K = 512
         const int pf_opt = option(ACCSPMM_OPT_PREFETCH);
         const bool pf = pf_opt == 1 || (pf_opt < 0 && (a.n_slices & 1u));
+        // the same rule for 160-byte slices: K = 64 (one slice) 1.040
+        // against 1.064 ms per adaptive step on the 1M-row matrix
+        const bool pf64 = pf;
         if (st == ACCSPMM_SUCCESS && fs == 32) {
             st = epi_on ? launch_packed_t<32, 4, 3, false, 2, true>(a, s) : launch_packed_t<32, 4, 3>(a, s);
         } else if (st == ACCSPMM_SUCCESS && fs == 64) {
             // two tiles in flight per warp at 3 CTAs per SM, the unpacked
             // 64-column default's shape
-            st = epi_on ? launch_packed_t<64, 2, 3, false, 2, true>(a, s) : launch_packed_t<64, 2, 3>(a, s);
+            if (epi_on)
+                st = launch_packed_t<64, 2, 3, false, 2, true>(a, s);
+            else
+                st = pf64 ? launch_packed_t<64, 2, 3, true>(a, s) : launch_packed_t<64, 2, 3>(a, s);
         } else if (st == ACCSPMM_SUCCESS && epi_on) {
             st = pf ? launch_packed_t<128, DirectBatch<128>::U, 2, true, 2, true>(a, s)
                     : launch_packed_t<128, DirectBatch<128>::U, 2, false, 2, true>(a, s);

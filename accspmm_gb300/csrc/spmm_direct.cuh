@@ -300,15 +300,17 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
         static_assert(!PF || (MA == 1 && 16 * U <= 32), "one prefetched row per lane");
         auto prefetch_rows = [&]() {
             if (PF && lane >= 8 * U && ma[0] < a.cols) {
-                static_assert(!PF || FS == 128, "the prefetch covers 320-byte slices");
-                const uint8_t* r = a.bp + size_t(ma[0]) * a.bpitch + 320 * (blk.f0 / 128);
+                static_assert(!PF || FS == 128 || FS == 64, "the prefetch covers 320- and 160-byte slices");
+                const uint8_t* r = a.bp + size_t(ma[0]) * a.bpitch + SB * (blk.f0 / FS);
                 if (PFK == 1) {
-                    asm volatile("cp.async.bulk.prefetch.L2.global [%0], 320;" ::"l"(r) : "memory");
+                    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(r), "n"(SB) : "memory");
                 } else {
-                    // the three 128-byte lines that hold the 320-byte slice
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(r));
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(r + 128));
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(r + 256));
+                    // the 128-byte lines that hold the slice: three for a
+                    // 320-byte slice (rows start on 64-byte boundaries), two
+                    // for a 160-byte one (32-byte boundaries)
+#pragma unroll
+                    for (int off = 0; off < SB; off += 128)
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(r + off));
                 }
             }
         };

@@ -250,9 +250,9 @@ void accspmm_adpbme_destroy(accspmm_adpbme_t* adp);
  * from the library's memory pool (released in stream order): the SpMM then
  * gathers 10 instead of 16 sectors of each 128-column row slice (5 of 8 of
  * a 64-column one, 3 of 4 of a 32-column one),
- * with bit-identical results, and at 128-column slices prefetches into L2
- * the rows of the tile group two ahead of the one it loads (when K spans an
- * odd number of 128-column slices).
+ * with bit-identical results, and at 128- and 64-column slices prefetches
+ * into L2 the rows of the tile group two ahead of the one it loads (when K
+ * spans an odd number of slices).
  * ACCSPMM_OPT_PACK and ACCSPMM_OPT_PREFETCH (accspmm_set_option) turn them
  * off or on. */
 int accspmm_spmm_tf32(const accspmm_metcf_t* metcf, const float* B, float* C,
@@ -456,8 +456,9 @@ enum {
     ACCSPMM_OPT_PREFETCH = 1,         /* ACCSPMM_PREFETCH (0 -> 0, 1 -> 1): -1 (default)
                                          the packed kernel prefetches into L2 the rows of
                                          the tile group two ahead when K spans an odd
-                                         number of 128-column slices (where it measured
-                                         faster); 0 never; 1 always */
+                                         number of its 128- or 64-column slices (where it
+                                         measured faster); 0 never; 1 always (32-column
+                                         slices never prefetch) */
     ACCSPMM_OPT_SCHEDULE = 2,         /* ACCSPMM_SCHEDULE: 1 (default) launches of a few
                                          waves run their window blocks heaviest first; 0 in
                                          window order */

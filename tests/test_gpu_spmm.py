@@ -705,7 +705,8 @@ def test_forced_packing_on_a_small_b_is_bit_identical(K):
     160-byte 64-column slices of the K <= 64 shape (K = 40, 64) and in the
     80-byte 32-column slices of the K <= 32 shape (K = 16, 32): ragged last
     slices, rows that are not a multiple of the window height, the plain and
-    adaptive entry points."""
+    adaptive entry points; with the L2 prefetch of rows two tile groups ahead
+    forced on and off (128- and 64-column slices)."""
     n = 5003
     rp, ci, vals = synth.powerlaw_local(n=n, seed=7)
     csr = dict(rows=n, cols=n, nnz=len(ci), row_ptr=rp, col_idx=ci, data=vals)
@@ -714,13 +715,14 @@ def test_forced_packing_on_a_small_b_is_bit_identical(K):
     cr = a.c_rows()
     dB = torch.rand((n, K), device="cuda") * 2 - 1
     out = {}
-    for pk in ("2", "0"):
-        with capi.option(capi.OPT_PACK, 1 if pk == "2" else 0):
+    for pk, pf in (("2", -1), ("0", -1), ("2", 1), ("2", 0)):
+        with capi.option(capi.OPT_PACK, 1 if pk == "2" else 0), capi.option(capi.OPT_PREFETCH, pf):
             C, Ca = empty_dev(m.c_rows, K), empty_dev(cr, K)
             m.spmm(dB, C, K)
             a.spmm(dB, Ca, cr, K)
             torch.cuda.synchronize()
-        out[pk] = (C, Ca)
-    assert torch.equal(out["2"][0], out["0"][0]) and torch.equal(out["2"][1], out["0"][1])
+        out[pk if pf < 0 else f"{pk}pf{pf}"] = (C, Ca)
+    for key in ("0", "2pf1", "2pf0"):
+        assert torch.equal(out["2"][0], out[key][0]) and torch.equal(out["2"][1], out[key][1]), key
     ref = oracle.spmm_csr_f64(rp, ci, vals, dB.cpu().numpy())
     assert rel_fro(out["2"][0][:n].cpu().numpy(), ref) < TOL_TF32_VS_F64
