@@ -826,8 +826,12 @@ int spmm_window_launch_slices(const uint32_t* rwo, const uint32_t* tc_offset, co
         // the same rule for 160-byte slices: K = 64 (one slice) 1.040
         // against 1.064 ms per adaptive step on the 1M-row matrix
         const bool pf64 = pf;
+        const bool pf32 = pf_opt == 1;
         if (st == ACCSPMM_SUCCESS && fs == 32) {
-            st = epi_on ? launch_packed_t<32, 4, 3, false, 2, true>(a, s) : launch_packed_t<32, 4, 3>(a, s);
+            if (epi_on)
+                st = launch_packed_t<32, 4, 3, false, 2, true>(a, s);
+            else
+                st = pf32 ? launch_packed_t<32, 4, 3, true>(a, s) : launch_packed_t<32, 4, 3>(a, s);
         } else if (st == ACCSPMM_SUCCESS && fs == 64) {
             // two tiles in flight per warp at 3 CTAs per SM, the unpacked
             // 64-column default's shape

@@ -211,7 +211,9 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
     constexpr int H = FS / 32;
     using L = Layout<H>;
     constexpr int NM = L::NM;
-    constexpr int MA = (8 * U + 31) / 32;             // a2b registers per lane
+    // a2b registers per lane: the group's 8U entries, and with PF the 8U of
+    // the group after (lanes 8U .. 16U - 1, or a register of their own at U = 4)
+    constexpr int MA = ((PF ? 16 : 8) * U + 31) / 32;
 
     const int lane = blk.lane, g = blk.g, tq = blk.tq;
     const uint32_t tb = blk.bound(blk.warp), te = blk.bound(blk.warp + 1);
@@ -232,7 +234,7 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
             for (int j = 0; j < MA; ++j) {
                 uint32_t e = 32 * j + lane;
                 uint32_t tile = t + e / 8;
-                // PF: lanes 8U .. 16U - 1 take the entries of the group after
+                // PF: entries 8U .. 16U - 1 are those of the group after
                 ma[j] = (e < (PF ? 16 * U : 8 * U) && tile < te) ? __ldg(a.a2b + size_t(t) * 8 + e) : kPad;
             }
             uint32_t tl = t + uint32_t(lane);
@@ -295,15 +297,23 @@ __device__ __forceinline__ void direct_item_packed(const SpmmArgs& a, const Bloc
                 n1[u] = ldg_u32_ordered(w1 + nb_off);
             }
         };
-        // PF: lane 8U + e holds sparseA2B entry e of the group after the one
-        // that load_meta fetched for issue, two groups ahead of the loads
-        static_assert(!PF || (MA == 1 && 16 * U <= 32), "one prefetched row per lane");
+        // PF: entry e of the group after the one that load_meta fetched for
+        // issue (two groups ahead of the loads) sits in lane 8U + e of ma[0]
+        // when 16U <= 32, else in lane e of ma[1]; each such lane prefetches
+        // that row's slice
+        static_assert(!PF || 16 * U == 32 || 8 * U == 32, "one prefetched row per lane");
+        constexpr int kPfReg = 8 * U >= 32 ? 1 : 0;
         auto prefetch_rows = [&]() {
-            if (PF && lane >= 8 * U && ma[0] < a.cols) {
-                static_assert(!PF || FS == 128 || FS == 64, "the prefetch covers 320- and 160-byte slices");
-                const uint8_t* r = a.bp + size_t(ma[0]) * a.bpitch + SB * (blk.f0 / FS);
+            const uint32_t e = ma[PF ? kPfReg : 0];
+            if (PF && (kPfReg == 1 || lane >= 8 * U) && e < a.cols) {
+                const uint8_t* r = a.bp + size_t(e) * a.bpitch + SB * (blk.f0 / FS);
                 if (PFK == 1) {
                     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(r), "n"(SB) : "memory");
+                } else if constexpr (FS == 32) {
+                    // an 80-byte slice starts on a 16-byte boundary: the
+                    // lines of its first and last bytes
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(r));
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(r + SB - 1));
                 } else {
                     // the 128-byte lines that hold the slice: three for a
                     // 320-byte slice (rows start on 64-byte boundaries), two

@@ -457,8 +457,8 @@ enum {
                                          the packed kernel prefetches into L2 the rows of
                                          the tile group two ahead when K spans an odd
                                          number of its 128- or 64-column slices (where it
-                                         measured faster); 0 never; 1 always (32-column
-                                         slices never prefetch) */
+                                         measured faster; never at 32-column slices, where
+                                         it measured slower); 0 never; 1 always */
     ACCSPMM_OPT_SCHEDULE = 2,         /* ACCSPMM_SCHEDULE: 1 (default) launches of a few
                                          waves run their window blocks heaviest first; 0 in
                                          window order */
