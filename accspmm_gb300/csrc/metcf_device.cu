@@ -3,8 +3,13 @@
 // (include/format.hpp:110-142, :215-274, :340-429; include/utils.hpp:75-85).
 //
 // METCF on the device:
-//  1. key = (window << colbits) | col for every CSR entry, value = CSR position;
-//     one stable radix sort orders entries by (window, column, position).
+//  1. every window's entries (contiguous in CSR order) are ordered by
+//     (column, CSR position) in place: a bitonic sort in shared memory per
+//     window of up to 2,048 entries; the entries of larger windows are
+//     gathered and ordered by one stable radix sort of the keys
+//     (window << colbits) | col.  Either way the result is the entries
+//     ordered by (window, column, position) with key = (window << colbits) |
+//     col and value = CSR position.
 //  2. unique-key flags, scanned, give each entry the rank of its column among
 //     the window's sorted distinct columns (include/format.hpp:179-199).
 //  3. tiles per window = ceil(distinct / 8), scanned -> rowWindowOffset.
@@ -38,23 +43,120 @@ int bits_for(uint64_t x) {
 // Error flags a kernel raises for malformed input (read back by the host).
 enum : uint32_t { kErrColRange = 1u, kErrRowPtr = 2u };
 
-__global__ void metcf_keys_kernel(const uint32_t* __restrict__ row_ptr,
-                                  const uint32_t* __restrict__ col_idx, uint32_t rows,
-                                  uint32_t cols, uint32_t W, int colbits,
-                                  uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
-                                  uint32_t* __restrict__ err) {
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t lane = threadIdx.x & 31;
-    if (warp >= W) return;
-    const uint32_t r0 = warp * kWin, r1 = min(r0 + kWin, rows);
-    const uint32_t s = row_ptr[r0], e = row_ptr[r1];
-    if (s > e && lane == 0) atomicOr(err, kErrRowPtr);
-    for (uint32_t i = s + lane; i < e; i += 32) {
-        uint32_t c = col_idx[i];
-        if (c >= cols) atomicOr(err, kErrColRange);
-        keys[i] = (uint64_t(warp) << colbits) | uint64_t(c);
-        vals[i] = i;
+// Entries of window w: [row_ptr[8w], row_ptr[min(8w + 8, rows)]), or none
+// when row_ptr is malformed there (flagged).
+__device__ __forceinline__ bool window_range(const uint32_t* __restrict__ row_ptr, uint32_t rows,
+                                             uint32_t nnz, uint32_t w, uint32_t* s, uint32_t* e,
+                                             uint32_t* __restrict__ err, bool report) {
+    const uint32_t r0 = w * kWin, r1 = min(r0 + kWin, rows);
+    *s = row_ptr[r0];
+    *e = row_ptr[r1];
+    if (*s > *e || *e > nnz) {
+        if (report) atomicOr(err, kErrRowPtr);
+        return false;
     }
+    return true;
+}
+
+constexpr uint32_t kSortSmall = 256;    // entries a window sorted by the small class may hold
+constexpr uint32_t kSortLarge = 2048;   // the largest window sorted in shared memory
+constexpr int kSortThreads = 128;
+
+// One block per window with lo < entries <= CAP: its (column, position)
+// pairs sorted ascending by a bitonic network in shared memory (the pairs
+// are distinct, so the order is the stable one), written as sorted keys and
+// CSR positions in the window's own range.  Windows of the class lo = 0
+// also check the row offsets and column indices.
+template <uint32_t CAP>
+__global__ void __launch_bounds__(kSortThreads)
+    window_sort_kernel(const uint32_t* __restrict__ row_ptr, const uint32_t* __restrict__ col_idx,
+                       uint32_t rows, uint32_t cols, uint32_t nnz, int colbits, uint32_t lo,
+                       uint64_t* __restrict__ skeys, uint32_t* __restrict__ svals,
+                       uint32_t* __restrict__ err) {
+    __shared__ uint64_t sk[CAP];
+    const uint32_t w = blockIdx.x;
+    uint32_t s, e;
+    if (!window_range(row_ptr, rows, nnz, w, &s, &e, err, lo == 0 && threadIdx.x == 0)) return;
+    const uint32_t n = e - s;
+    if (n <= lo || n > CAP) return;
+    uint32_t P = 1;
+    while (P < n) P <<= 1;
+    bool bad = false;
+    for (uint32_t j = threadIdx.x; j < P; j += kSortThreads) {
+        uint64_t v = ~0ull;
+        if (j < n) {
+            const uint32_t c = col_idx[s + j];
+            bad |= c >= cols;
+            v = (uint64_t(c) << 32) | j;
+        }
+        sk[j] = v;
+    }
+    if (bad) atomicOr(err, kErrColRange);
+    __syncthreads();
+    for (uint32_t k = 2; k <= P; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = threadIdx.x; i < P; i += kSortThreads) {
+                const uint32_t x = i ^ j;
+                if (x > i) {
+                    const uint64_t a = sk[i], b = sk[x];
+                    if ((a > b) == ((i & k) == 0)) {
+                        sk[i] = b;
+                        sk[x] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    const uint64_t wk = uint64_t(w) << colbits;
+    for (uint32_t j = threadIdx.x; j < n; j += kSortThreads) {
+        const uint64_t v = sk[j];
+        skeys[s + j] = wk | (v >> 32);
+        svals[s + j] = s + uint32_t(v);
+    }
+}
+
+// Entries of windows above kSortLarge (valid ones), 0 for the others.
+__global__ void large_window_sizes_kernel(const uint32_t* __restrict__ row_ptr, uint32_t rows,
+                                          uint32_t nnz, uint32_t W, uint32_t* __restrict__ sizes) {
+    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
+    uint32_t s, e;
+    const bool ok = window_range(row_ptr, rows, nnz, w, &s, &e, nullptr, false);
+    sizes[w] = ok && e - s > kSortLarge ? e - s : 0u;
+}
+
+// One warp per large window: its keys and CSR positions, gathered at the
+// window's offset in the compact arrays (dir 0), or the sorted compact
+// pairs written back to the window's range (dir 1).
+__global__ void large_window_move_kernel(const uint32_t* __restrict__ row_ptr,
+                                         const uint32_t* __restrict__ col_idx, uint32_t rows,
+                                         uint32_t cols, uint32_t W, int colbits,
+                                         const uint32_t* __restrict__ sizes,
+                                         const uint32_t* __restrict__ offs, int dir,
+                                         uint64_t* __restrict__ ckeys, uint32_t* __restrict__ cvals,
+                                         uint64_t* __restrict__ skeys, uint32_t* __restrict__ svals,
+                                         uint32_t* __restrict__ err) {
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31;
+    if (w >= W) return;
+    const uint32_t n = sizes[w];
+    if (n == 0) return;
+    const uint32_t s = row_ptr[w * kWin], o = offs[w];
+    const uint64_t wk = uint64_t(w) << colbits;
+    bool bad = false;
+    for (uint32_t k = lane; k < n; k += 32) {
+        if (dir == 0) {
+            const uint32_t c = col_idx[s + k];
+            bad |= c >= cols;
+            ckeys[o + k] = wk | c;
+            cvals[o + k] = s + k;
+        } else {
+            skeys[s + k] = ckeys[o + k];
+            svals[s + k] = cvals[o + k];
+        }
+    }
+    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(err, kErrColRange);
 }
 
 __global__ void uniq_flags_kernel(const uint64_t* __restrict__ skeys, uint32_t n,
@@ -66,11 +168,12 @@ __global__ void uniq_flags_kernel(const uint64_t* __restrict__ skeys, uint32_t n
 // E = exclusive scan of the unique flags.  Window w's sorted entries occupy
 // [row_ptr[8w], row_ptr[8w+8]) because the sort key starts with the window.
 __global__ void window_tiles_kernel(const uint32_t* __restrict__ row_ptr, uint32_t rows,
-                                    uint32_t W, const uint32_t* __restrict__ E,
+                                    uint32_t nnz, uint32_t W, const uint32_t* __restrict__ E,
                                     uint32_t* __restrict__ tiles) {
     uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= W) return;
-    uint32_t s = row_ptr[w * kWin], e = row_ptr[min(w * kWin + kWin, rows)];
+    // malformed offsets (reported by the sort) count no entries here
+    uint32_t e = min(row_ptr[min(w * kWin + kWin, rows)], nnz), s = min(row_ptr[w * kWin], e);
     uint32_t u = E[e] - E[s];
     tiles[w] = (u + kWin - 1) / kWin;
 }
@@ -348,6 +451,49 @@ __global__ void coo_gather_kernel(const uint32_t* __restrict__ perm, uint32_t nn
 
 inline unsigned blocks_for(size_t n, unsigned threads) { return unsigned((n + threads - 1) / threads); }
 
+// Orders every window's entries by (column, CSR position) into skeys /
+// svals (keys (window << colbits) | col, values CSR positions): windows of
+// up to 256 and up to 2,048 entries sorted in shared memory, larger windows
+// gathered into compact arrays, radix-sorted together and written back.
+int sort_window_entries(const accspmm_csr_t* csr, uint32_t W, int colbits, int wbits, uint64_t* skeys,
+                        uint32_t* svals, uint32_t* err, cudaStream_t s) {
+    if (W == 0) return ACCSPMM_SUCCESS;
+    const uint32_t rows = csr->rows, cols = csr->cols, nnz = csr->nnz;
+    window_sort_kernel<kSortSmall><<<W, kSortThreads, 0, s>>>(csr->row_ptr, csr->col_idx, rows, cols, nnz,
+                                                             colbits, 0, skeys, svals, err);
+    ACC_LAUNCH_CHECK();
+    window_sort_kernel<kSortLarge><<<W, kSortThreads, 0, s>>>(csr->row_ptr, csr->col_idx, rows, cols, nnz,
+                                                             colbits, kSortSmall, skeys, svals, err);
+    ACC_LAUNCH_CHECK();
+    DevBuf<uint32_t> sizes, offs;
+    ACC_CUDA(sizes.alloc(W, s));
+    ACC_CUDA(offs.alloc(size_t(W) + 1, s));
+    large_window_sizes_kernel<<<blocks_for(W, 256), 256, 0, s>>>(csr->row_ptr, rows, nnz, W, sizes.p);
+    ACC_LAUNCH_CHECK();
+    int st = scan_exclusive_u32(sizes.p, offs.p, W, s);
+    if (st) return st;
+    uint32_t L = 0;
+    ACC_CUDA(cudaMemcpyAsync(&L, offs.p + W, 4, cudaMemcpyDeviceToHost, s));
+    ACC_CUDA(cudaStreamSynchronize(s));
+    if (L == 0) return ACCSPMM_SUCCESS;
+    DevBuf<uint64_t> ck, cks;
+    DevBuf<uint32_t> cv, cvs;
+    ACC_CUDA(ck.alloc(L, s));
+    ACC_CUDA(cv.alloc(L, s));
+    ACC_CUDA(cks.alloc(L, s));
+    ACC_CUDA(cvs.alloc(L, s));
+    const unsigned grid = blocks_for(size_t(W) * 32, 256);
+    large_window_move_kernel<<<grid, 256, 0, s>>>(csr->row_ptr, csr->col_idx, rows, cols, W, colbits, sizes.p,
+                                                  offs.p, 0, ck.p, cv.p, nullptr, nullptr, err);
+    ACC_LAUNCH_CHECK();
+    st = radix_sort_pairs(ck.p, cv.p, cks.p, cvs.p, L, colbits + wbits, s);
+    if (st) return st;
+    large_window_move_kernel<<<grid, 256, 0, s>>>(csr->row_ptr, csr->col_idx, rows, cols, W, colbits, sizes.p,
+                                                  offs.p, 1, cks.p, cvs.p, skeys, svals, err);
+    ACC_LAUNCH_CHECK();
+    return ACCSPMM_SUCCESS;
+}
+
 }  // namespace
 
 int metcf_from_csr_device(const accspmm_csr_t* csr, accspmm_metcf_t* out, void* stream) {
@@ -359,26 +505,17 @@ int metcf_from_csr_device(const accspmm_csr_t* csr, accspmm_metcf_t* out, void* 
     const int wbits = bits_for(W ? W - 1 : 0);
     if (colbits + wbits > 64) ACC_FAIL(ACCSPMM_ERROR_OVERFLOW, "matrix too large for 64-bit keys");
 
-    DevBuf<uint64_t> keys, skeys;
-    DevBuf<uint32_t> vals, svals, flags, E, tiles, err;
+    DevBuf<uint64_t> skeys;
+    DevBuf<uint32_t> svals, flags, E, tiles, err;
     DevBuf<uint32_t> rwo, tc_offset, a2b, counts, seg;
     DevBuf<uint64_t> bits;
     DevBuf<float> data;
     ACC_CUDA(err.alloc(1, s));
     ACC_CUDA(cudaMemsetAsync(err.p, 0, 4, s));
-    ACC_CUDA(keys.alloc(nnz, s));
-    ACC_CUDA(vals.alloc(nnz, s));
-    if (W) {
-        metcf_keys_kernel<<<blocks_for(size_t(W) * 32, 256), 256, 0, s>>>(
-            csr->row_ptr, csr->col_idx, rows, cols, W, colbits, keys.p, vals.p, err.p);
-        ACC_LAUNCH_CHECK();
-    }
     ACC_CUDA(skeys.alloc(nnz, s));
     ACC_CUDA(svals.alloc(nnz, s));
-    int st = radix_sort_pairs(keys.p, vals.p, skeys.p, svals.p, nnz, colbits + wbits, s);
+    int st = sort_window_entries(csr, W, colbits, wbits, skeys.p, svals.p, err.p, s);
     if (st) return st;
-    keys.reset();
-    vals.reset();
     ACC_CUDA(flags.alloc(nnz, s));
     ACC_CUDA(E.alloc(size_t(nnz) + 1, s));
     if (nnz) {
@@ -391,7 +528,7 @@ int metcf_from_csr_device(const accspmm_csr_t* csr, accspmm_metcf_t* out, void* 
     ACC_CUDA(tiles.alloc(W, s));
     ACC_CUDA(rwo.alloc(size_t(W) + 1, s));
     if (W) {
-        window_tiles_kernel<<<blocks_for(W, 256), 256, 0, s>>>(csr->row_ptr, rows, W, E.p, tiles.p);
+        window_tiles_kernel<<<blocks_for(W, 256), 256, 0, s>>>(csr->row_ptr, rows, nnz, W, E.p, tiles.p);
         ACC_LAUNCH_CHECK();
     }
     st = scan_exclusive_u32(tiles.p, rwo.p, W, s);
