@@ -95,14 +95,14 @@ __global__ void __launch_bounds__(kSortThreads)
     __syncthreads();
     for (uint32_t k = 2; k <= P; k <<= 1) {
         for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = threadIdx.x; i < P; i += kSortThreads) {
-                const uint32_t x = i ^ j;
-                if (x > i) {
-                    const uint64_t a = sk[i], b = sk[x];
-                    if ((a > b) == ((i & k) == 0)) {
-                        sk[i] = b;
-                        sk[x] = a;
-                    }
+            // pair q compares i (bit j clear: q with a zero inserted at
+            // bit j) with i + j
+            for (uint32_t q = threadIdx.x; q < P / 2; q += kSortThreads) {
+                const uint32_t i = ((q & ~(j - 1)) << 1) | (q & (j - 1)), x = i + j;
+                const uint64_t a = sk[i], b = sk[x];
+                if ((a > b) == ((i & k) == 0)) {
+                    sk[i] = b;
+                    sk[x] = a;
                 }
             }
             __syncthreads();
@@ -126,37 +126,36 @@ __global__ void large_window_sizes_kernel(const uint32_t* __restrict__ row_ptr, 
     sizes[w] = ok && e - s > kSortLarge ? e - s : 0u;
 }
 
-// One warp per large window: its keys and CSR positions, gathered at the
-// window's offset in the compact arrays (dir 0), or the sorted compact
-// pairs written back to the window's range (dir 1).
+// One thread per entry of the large windows (compact index j; offs is the
+// exclusive scan of their sizes): the entry's key and CSR position gathered
+// to the compact arrays (dir 0), or the sorted compact pair j written back to
+// its window's range (dir 1).
 __global__ void large_window_move_kernel(const uint32_t* __restrict__ row_ptr,
-                                         const uint32_t* __restrict__ col_idx, uint32_t rows,
-                                         uint32_t cols, uint32_t W, int colbits,
-                                         const uint32_t* __restrict__ sizes,
-                                         const uint32_t* __restrict__ offs, int dir,
-                                         uint64_t* __restrict__ ckeys, uint32_t* __restrict__ cvals,
-                                         uint64_t* __restrict__ skeys, uint32_t* __restrict__ svals,
-                                         uint32_t* __restrict__ err) {
-    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t lane = threadIdx.x & 31;
-    if (w >= W) return;
-    const uint32_t n = sizes[w];
-    if (n == 0) return;
-    const uint32_t s = row_ptr[w * kWin], o = offs[w];
-    const uint64_t wk = uint64_t(w) << colbits;
-    bool bad = false;
-    for (uint32_t k = lane; k < n; k += 32) {
-        if (dir == 0) {
-            const uint32_t c = col_idx[s + k];
-            bad |= c >= cols;
-            ckeys[o + k] = wk | c;
-            cvals[o + k] = s + k;
-        } else {
-            skeys[s + k] = ckeys[o + k];
-            svals[s + k] = cvals[o + k];
-        }
+                                         const uint32_t* __restrict__ col_idx, uint32_t cols,
+                                         uint32_t W, int colbits, const uint32_t* __restrict__ offs,
+                                         uint32_t L, int dir, uint64_t* __restrict__ ckeys,
+                                         uint32_t* __restrict__ cvals, uint64_t* __restrict__ skeys,
+                                         uint32_t* __restrict__ svals, uint32_t* __restrict__ err) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= L) return;
+    // the window holding j: the last w with offs[w] <= j (windows of size
+    // zero share their successor's offset)
+    uint32_t lo = 0, hi = W;  // offs[lo] <= j < offs[hi + 1]
+    while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo + 1) / 2;
+        if (offs[mid] <= j) lo = mid;
+        else hi = mid - 1;
     }
-    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(err, kErrColRange);
+    const uint32_t w = lo, k = j - offs[w], s = row_ptr[w * kWin];
+    if (dir == 0) {
+        const uint32_t c = col_idx[s + k];
+        if (c >= cols) atomicOr(err, kErrColRange);
+        ckeys[j] = (uint64_t(w) << colbits) | c;
+        cvals[j] = s + k;
+    } else {
+        skeys[s + k] = ckeys[j];
+        svals[s + k] = cvals[j];
+    }
 }
 
 __global__ void uniq_flags_kernel(const uint64_t* __restrict__ skeys, uint32_t n,
@@ -482,14 +481,14 @@ int sort_window_entries(const accspmm_csr_t* csr, uint32_t W, int colbits, int w
     ACC_CUDA(cv.alloc(L, s));
     ACC_CUDA(cks.alloc(L, s));
     ACC_CUDA(cvs.alloc(L, s));
-    const unsigned grid = blocks_for(size_t(W) * 32, 256);
-    large_window_move_kernel<<<grid, 256, 0, s>>>(csr->row_ptr, csr->col_idx, rows, cols, W, colbits, sizes.p,
-                                                  offs.p, 0, ck.p, cv.p, nullptr, nullptr, err);
+    const unsigned grid = blocks_for(L, 256);
+    large_window_move_kernel<<<grid, 256, 0, s>>>(csr->row_ptr, csr->col_idx, cols, W, colbits, offs.p, L, 0,
+                                                  ck.p, cv.p, nullptr, nullptr, err);
     ACC_LAUNCH_CHECK();
     st = radix_sort_pairs(ck.p, cv.p, cks.p, cvs.p, L, colbits + wbits, s);
     if (st) return st;
-    large_window_move_kernel<<<grid, 256, 0, s>>>(csr->row_ptr, csr->col_idx, rows, cols, W, colbits, sizes.p,
-                                                  offs.p, 1, cks.p, cvs.p, skeys, svals, err);
+    large_window_move_kernel<<<grid, 256, 0, s>>>(csr->row_ptr, csr->col_idx, cols, W, colbits, offs.p, L, 1,
+                                                  cks.p, cvs.p, skeys, svals, err);
     ACC_LAUNCH_CHECK();
     return ACCSPMM_SUCCESS;
 }

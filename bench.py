@@ -256,7 +256,7 @@ def peaks():
 # the reason).
 KERNEL_SOURCES = ("accspmm_gb300/csrc/spmm.cu", "accspmm_gb300/csrc/spmm_direct.cuh",
                   "accspmm_gb300/csrc/spmm_common.cuh")
-TRAFFIC = {128: {"bytes": 8052843336, "src_sha": "728b247c4631918a",
+TRAFFIC = {128: {"bytes": 8061555544, "src_sha": "b5d7599577741483",
                  "capture": "profiles/spmm_window_packed_kernel_powerlaw_local.md"}}
 
 

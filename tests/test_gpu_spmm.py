@@ -111,6 +111,38 @@ def test_device_metcf_config1_and_unsorted(seed):
         np.testing.assert_array_equal(h[k], o[k], err_msg=k)
 
 
+def test_device_metcf_windows_of_every_sort_class():
+    """The device builder orders each window's entries in shared memory when
+    the window holds up to 256 or up to 2,048 entries, and gathers larger
+    windows for a radix sort: windows of 1, 200, 1,500, 2,048, 2,049 and
+    about 9,000 entries (rows in random column order with duplicates, one row
+    alone holding 6,000 entries), next to empty windows, give the oracle's
+    arrays."""
+    rng = np.random.default_rng(11)
+    rows, cols = 3001, 20000
+    per_window = {0: 1, 1: 200, 2: 1500, 3: 2048, 4: 2049, 6: 9000, 9: 0, 10: 37}
+    rr, cc = [], []
+    for w, n in per_window.items():
+        if w == 6:
+            counts = [6000, 500, 500, 500, 500, 400, 400, 200]
+        else:
+            counts = np.bincount(rng.integers(0, 8, n), minlength=8)
+        for r, k in enumerate(counts):
+            rr.append(np.full(k, 8 * w + r, np.uint32))
+            cc.append(rng.integers(0, cols, k).astype(np.uint32))  # duplicates included
+    rr.append(rng.integers(100, rows, 5000).astype(np.uint32))
+    cc.append(rng.integers(0, cols, 5000).astype(np.uint32))
+    rr, cc = np.concatenate(rr), np.concatenate(cc)
+    perm = rng.permutation(len(rr))
+    rr, cc = rr[perm], cc[perm]
+    vv = rng.random(len(rr), dtype=np.float32)
+    csr = api.csr_from_coo(rows, cols, rr, cc, vv)
+    o = oracle.metcf(rows, csr["row_ptr"], csr["col_idx"], csr["data"])
+    h = device_metcf(csr).to_numpy()
+    for k in ("rwo", "tc_offset", "bits", "a2b", "data"):
+        np.testing.assert_array_equal(h[k], o[k], err_msg=k)
+
+
 def spmm_plain(m, B, K, prec=capi.PREC_TF32):
     dB = torch_dev(B)
     dC = empty_dev(m.c_rows, K)
