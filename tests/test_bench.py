@@ -1,6 +1,7 @@
 """bench.py's host logic without a GPU: the compulsory-byte model, the
-reference arm (the CPU CSR SpMM on a small workload) and the replica
-aggregation across ranks (two gloo processes on CPU)."""
+reference arm (the CPU CSR SpMM on a small workload), the replica
+aggregation across ranks (two gloo processes on CPU), the DRAM-traffic
+figure keyed by the kernel sources, and the clock summary."""
 import json
 import os
 import subprocess
@@ -76,3 +77,26 @@ def test_reference_kernel_launch_config():
     import torch
     if not torch.cuda.is_available():
         assert ref_gpu.available() is not None
+
+
+def test_measured_traffic_is_keyed_by_the_kernel_sources(monkeypatch):
+    """roofline.traffic is reported only while the kernel sources hash to the
+    value its ncu capture was taken on; otherwise null with the reason."""
+    got, src = bench.measured_traffic(128)
+    assert got == bench.TRAFFIC[128]["bytes"] and bench.TRAFFIC[128]["src_sha"] in src
+    monkeypatch.setattr(bench, "kernel_source_hash", lambda: "0000000000000000")
+    got, src = bench.measured_traffic(128)
+    assert got is None and src.startswith("stale")
+    got, src = bench.measured_traffic(64)
+    assert got is None and "no ncu capture" in src
+
+
+def test_clock_summary_takes_the_median_and_every_reason():
+    c = bench.ClockSampler(0)
+    c.source = "test"
+    assert c.summary()["samples"] == 0
+    c.samples = [(2070.0, 2070.0, set()), (1900.0, 2070.0, {"sw_power_cap"}), (2070.0, 2070.0, set()),
+                 (1500.0, 2070.0, {"hw_slowdown", "sw_power_cap"})]
+    s = c.summary()
+    assert s["sm_mhz"] == 1985.0 and s["sm_max_mhz"] == 2070.0 and s["samples"] == 4
+    assert s["reasons"] == ["hw_slowdown", "sw_power_cap"]
