@@ -532,11 +532,15 @@ int metcf_from_csr_device(const accspmm_csr_t* csr, accspmm_metcf_t* out, void* 
     }
     st = scan_exclusive_u32(tiles.p, rwo.p, W, s);
     if (st) return st;
-    uint32_t host_T = 0, host_err = 0, host_nnz_end = 0;
+    uint32_t host_T = 0, host_err = 0, host_nnz_end = 0, host_first = 0;
     ACC_CUDA(cudaMemcpyAsync(&host_T, rwo.p + W, 4, cudaMemcpyDeviceToHost, s));
     ACC_CUDA(cudaMemcpyAsync(&host_err, err.p, 4, cudaMemcpyDeviceToHost, s));
     ACC_CUDA(cudaMemcpyAsync(&host_nnz_end, csr->row_ptr + rows, 4, cudaMemcpyDeviceToHost, s));
+    ACC_CUDA(cudaMemcpyAsync(&host_first, csr->row_ptr, 4, cudaMemcpyDeviceToHost, s));
     ACC_CUDA(cudaStreamSynchronize(s));
+    // entries outside every window (before row_ptr[0]) would have no sorted
+    // key: refused before any kernel reads the sorted entries by position
+    if (host_first != 0) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "row_ptr[0]=%u, not 0", host_first);
     if (host_nnz_end != nnz) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "row_ptr[rows]=%u but nnz=%u", host_nnz_end, nnz);
     if (host_err & kErrRowPtr) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "row_ptr is not non-decreasing");
     if (host_err & kErrColRange) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "column index >= cols");

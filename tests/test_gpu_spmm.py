@@ -143,6 +143,33 @@ def test_device_metcf_windows_of_every_sort_class():
         np.testing.assert_array_equal(h[k], o[k], err_msg=k)
 
 
+@pytest.mark.parametrize("case", ["column_past_cols", "window_start_after_its_end", "first_offset_not_zero",
+                                  "last_offset_short", "last_offset_past_nnz"])
+def test_device_metcf_refuses_a_malformed_csr(case):
+    """A device CSR whose column indices or row offsets are inconsistent is
+    refused with ACCSPMM_ERROR_INVALID_VALUE (every kernel of the build keeps
+    its reads and writes inside the arrays; the host checks the flags they
+    raise before any kernel indexes by the sorted entries)."""
+    n = 4096
+    rp, ci, v = synth.powerlaw_local(n=n, seed=2)
+    rp, ci = rp.astype(np.uint32).copy(), ci.astype(np.uint32).copy()
+    nnz = len(ci)
+    if case == "column_past_cols":
+        ci[100] = n + 5
+    elif case == "window_start_after_its_end":
+        rp[8] = rp[16] + 1  # window 1 (rows 8..15) would start after it ends
+    elif case == "first_offset_not_zero":
+        rp[0] = 1
+    elif case == "last_offset_short":
+        rp[-1] = nnz - 3
+    else:
+        rp[-1] = nnz + 3
+    d = api.DeviceCSR.upload(dict(rows=n, cols=n, nnz=nnz, row_ptr=rp, col_idx=ci, data=v))
+    with pytest.raises(capi.AccSpmmError) as e:
+        api.DeviceMETCF.from_csr(d)
+    assert e.value.status == capi.ERROR_INVALID_VALUE
+
+
 def spmm_plain(m, B, K, prec=capi.PREC_TF32):
     dB = torch_dev(B)
     dC = empty_dev(m.c_rows, K)
