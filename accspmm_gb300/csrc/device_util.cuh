@@ -31,7 +31,12 @@ inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 // Number of SMs of the current device (cached per device).
 int sm_count();
 
-// Stream-ordered device buffer that frees itself at scope exit.
+// The current device's library memory pool (spmm_host.cpp): it keeps freed
+// memory for later allocations instead of returning it at each synchronize.
+int library_pool(cudaMemPool_t* pool);
+
+// Stream-ordered device buffer from the library pool that frees itself at
+// scope exit.
 template <class T>
 struct DevBuf {
     T* p = nullptr;
@@ -43,6 +48,11 @@ struct DevBuf {
     cudaError_t alloc(size_t n, cudaStream_t st) {
         reset();
         s = st;
+        cudaMemPool_t pool;
+        if (library_pool(&pool) == ACCSPMM_SUCCESS)
+            return cudaMallocFromPoolAsync(reinterpret_cast<void**>(&p), sizeof(T) * (n ? n : 1), pool, st);
+        // no library pool (it could not be created here): the device's
+        // current pool
         return cudaMallocAsync(reinterpret_cast<void**>(&p), sizeof(T) * (n ? n : 1), st);
     }
     void reset() {

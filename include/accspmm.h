@@ -154,7 +154,10 @@ int accspmm_csr_from_coo(const accspmm_coo_t* coo, accspmm_csr_t* csr,
 
 /* METCFBit<T>::convertFromCSR, include/format.hpp:215-274.  Bit-exact with
  * the reference layout.  Host CSR -> host METCF on all host threads; device
- * CSR -> device METCF built by CUDA kernels on `stream`. */
+ * CSR -> device METCF built by CUDA kernels on `stream`.  The device
+ * builders' temporaries (about 24 bytes a nonzero at their peak) come from
+ * the library's memory pool per device, which keeps freed memory for later
+ * calls instead of returning it at each synchronize. */
 int accspmm_metcf_from_csr(const accspmm_csr_t* csr, accspmm_metcf_t* metcf,
                            void* stream);
 
