@@ -66,14 +66,19 @@ constexpr int kSortThreads = 128;
 // pairs sorted ascending by a bitonic network in shared memory (the pairs
 // are distinct, so the order is the stable one), written as sorted keys and
 // CSR positions in the window's own range.  Windows of the class lo = 0
-// also check the row offsets and column indices.
-template <uint32_t CAP>
+// also check the row offsets and column indices.  Key: the column above
+// the position in the window, 32 bits when colbits + log2(CAP) <= 32,
+// else 64.
+template <uint32_t CAP, typename Key>
 __global__ void __launch_bounds__(kSortThreads)
     window_sort_kernel(const uint32_t* __restrict__ row_ptr, const uint32_t* __restrict__ col_idx,
                        uint32_t rows, uint32_t cols, uint32_t nnz, int colbits, uint32_t lo,
                        uint64_t* __restrict__ skeys, uint32_t* __restrict__ svals,
                        uint32_t* __restrict__ err) {
-    __shared__ uint64_t sk[CAP];
+    static_assert((CAP & (CAP - 1)) == 0, "power-of-two window class");
+    constexpr int RB = sizeof(Key) == 8 ? 32 : (CAP == 256 ? 8 : 11);  // position bits
+    static_assert(sizeof(Key) == 8 || (1u << RB) == CAP, "position field holds 0 .. CAP - 1");
+    __shared__ Key sk[CAP];
     const uint32_t w = blockIdx.x;
     uint32_t s, e;
     if (!window_range(row_ptr, rows, nnz, w, &s, &e, err, lo == 0 && threadIdx.x == 0)) return;
@@ -83,11 +88,13 @@ __global__ void __launch_bounds__(kSortThreads)
     while (P < n) P <<= 1;
     bool bad = false;
     for (uint32_t j = threadIdx.x; j < P; j += kSortThreads) {
-        uint64_t v = ~0ull;
+        // padding sorts last: a real key is below all ones, as j < n - 1
+        // < P - 1 wherever padding exists
+        Key v = ~Key(0);
         if (j < n) {
             const uint32_t c = col_idx[s + j];
             bad |= c >= cols;
-            v = (uint64_t(c) << 32) | j;
+            v = (Key(c) << RB) | Key(j);
         }
         sk[j] = v;
     }
@@ -99,7 +106,7 @@ __global__ void __launch_bounds__(kSortThreads)
             // bit j) with i + j
             for (uint32_t q = threadIdx.x; q < P / 2; q += kSortThreads) {
                 const uint32_t i = ((q & ~(j - 1)) << 1) | (q & (j - 1)), x = i + j;
-                const uint64_t a = sk[i], b = sk[x];
+                const Key a = sk[i], b = sk[x];
                 if ((a > b) == ((i & k) == 0)) {
                     sk[i] = b;
                     sk[x] = a;
@@ -110,9 +117,9 @@ __global__ void __launch_bounds__(kSortThreads)
     }
     const uint64_t wk = uint64_t(w) << colbits;
     for (uint32_t j = threadIdx.x; j < n; j += kSortThreads) {
-        const uint64_t v = sk[j];
-        skeys[s + j] = wk | (v >> 32);
-        svals[s + j] = s + uint32_t(v);
+        const Key v = sk[j];
+        skeys[s + j] = wk | uint64_t(v >> RB);
+        svals[s + j] = s + uint32_t(v & ((Key(1) << RB) - 1));
     }
 }
 
@@ -458,11 +465,20 @@ int sort_window_entries(const accspmm_csr_t* csr, uint32_t W, int colbits, int w
                         uint32_t* svals, uint32_t* err, cudaStream_t s) {
     if (W == 0) return ACCSPMM_SUCCESS;
     const uint32_t rows = csr->rows, cols = csr->cols, nnz = csr->nnz;
-    window_sort_kernel<kSortSmall><<<W, kSortThreads, 0, s>>>(csr->row_ptr, csr->col_idx, rows, cols, nnz,
-                                                             colbits, 0, skeys, svals, err);
-    ACC_LAUNCH_CHECK();
-    window_sort_kernel<kSortLarge><<<W, kSortThreads, 0, s>>>(csr->row_ptr, csr->col_idx, rows, cols, nnz,
-                                                             colbits, kSortSmall, skeys, svals, err);
+    // 32-bit keys while a column and an 11-bit position fit (cols <= 2^21)
+    if (colbits + 11 <= 32) {
+        window_sort_kernel<kSortSmall, uint32_t><<<W, kSortThreads, 0, s>>>(
+            csr->row_ptr, csr->col_idx, rows, cols, nnz, colbits, 0, skeys, svals, err);
+        ACC_LAUNCH_CHECK();
+        window_sort_kernel<kSortLarge, uint32_t><<<W, kSortThreads, 0, s>>>(
+            csr->row_ptr, csr->col_idx, rows, cols, nnz, colbits, kSortSmall, skeys, svals, err);
+    } else {
+        window_sort_kernel<kSortSmall, uint64_t><<<W, kSortThreads, 0, s>>>(
+            csr->row_ptr, csr->col_idx, rows, cols, nnz, colbits, 0, skeys, svals, err);
+        ACC_LAUNCH_CHECK();
+        window_sort_kernel<kSortLarge, uint64_t><<<W, kSortThreads, 0, s>>>(
+            csr->row_ptr, csr->col_idx, rows, cols, nnz, colbits, kSortSmall, skeys, svals, err);
+    }
     ACC_LAUNCH_CHECK();
     DevBuf<uint32_t> sizes, offs;
     ACC_CUDA(sizes.alloc(W, s));

@@ -111,15 +111,17 @@ def test_device_metcf_config1_and_unsorted(seed):
         np.testing.assert_array_equal(h[k], o[k], err_msg=k)
 
 
-def test_device_metcf_windows_of_every_sort_class():
+@pytest.mark.parametrize("cols", [20000, 3_000_000])
+def test_device_metcf_windows_of_every_sort_class(cols):
     """The device builder orders each window's entries in shared memory when
     the window holds up to 256 or up to 2,048 entries, and gathers larger
     windows for a radix sort: windows of 1, 200, 1,500, 2,048, 2,049 and
     about 9,000 entries (rows in random column order with duplicates, one row
     alone holding 6,000 entries), next to empty windows, give the oracle's
-    arrays."""
+    arrays; with 32-bit sort keys (20,000 columns) and 64-bit ones (3,000,000
+    columns, past the 2^21 a 32-bit key holds beside an 11-bit position)."""
     rng = np.random.default_rng(11)
-    rows, cols = 3001, 20000
+    rows = 3001
     per_window = {0: 1, 1: 200, 2: 1500, 3: 2048, 4: 2049, 6: 9000, 9: 0, 10: 37}
     rr, cc = [], []
     for w, n in per_window.items():
