@@ -145,8 +145,33 @@ int ServerImpl::issue(std::vector<std::shared_ptr<Request>>& take, int slot, uin
     b->reqs = take;
     const size_t n = take.size();
     *passes = 0;
+    // On a failure part of the batch may already be enqueued (copies into
+    // C_host among them): wait for the slot's stream, so that nothing still
+    // writes a caller's buffer once its request reports the failure, then
+    // free the buffers whose stream-ordered frees were not enqueued.
+    auto bail = [&](int code) {
+        cudaStreamSynchronize(st);
+        for (auto& r : take) {
+            for (float** q : {&r->dB, &r->dC, &r->dT})
+                if (*q) {
+                    cudaFree(*q);
+                    *q = nullptr;
+                }
+        }
+        if (b->d_desc) cudaFree(b->d_desc);
+        b->d_desc = nullptr;
+        return code;
+    };
+#define SERVER_FAIL(code, ...)             \
+    do {                                   \
+        ::accspmm::set_error(__VA_ARGS__); \
+        return bail(code);                 \
+    } while (0)
     cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&b->d_desc), sizeof(BatchDesc) * 2 * n + 16, st);
-    if (e != cudaSuccess) ACC_FAIL(ACCSPMM_ERROR_ALLOC, "descriptor allocation: %s", cudaGetErrorString(e));
+    if (e != cudaSuccess) {
+        b->d_desc = nullptr;
+        SERVER_FAIL(ACCSPMM_ERROR_ALLOC, "descriptor allocation: %s", cudaGetErrorString(e));
+    }
     b->d_counter = reinterpret_cast<uint32_t*>(b->d_desc + 2 * n);
     std::vector<BatchInput> in(n);
     for (size_t i = 0; i < n; ++i) {
@@ -156,7 +181,7 @@ int ServerImpl::issue(std::vector<std::shared_ptr<Request>>& take, int slot, uin
         if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&r.dC), r.bytes_C, st);
         if (e == cudaSuccess && r.bytes_T) e = cudaMallocAsync(reinterpret_cast<void**>(&r.dT), r.bytes_T, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(r.dB, r.B_host, r.bytes_B, cudaMemcpyHostToDevice, st);
-        if (e != cudaSuccess) ACC_FAIL(ACCSPMM_ERROR_CUDA, "request buffers: %s", cudaGetErrorString(e));
+        if (e != cudaSuccess) SERVER_FAIL(ACCSPMM_ERROR_CUDA, "request buffers: %s", cudaGetErrorString(e));
         // the first layer of a chain writes the temporary, else C
         in[i] = BatchInput{m.row_window_offset, m.tc_offset, m.tc_local_bit, m.sparse_a2b, m.data,
                            r.dB, r.chain == 2 ? r.dT : r.dC, m.num_windows, m.num_windows,
@@ -164,7 +189,7 @@ int ServerImpl::issue(std::vector<std::shared_ptr<Request>>& take, int slot, uin
     }
     BatchDesc* stg = staging[slot];
     int rc = enqueue_pass(in, take[0]->precision, stg, b->d_desc, b->d_counter, st);
-    if (rc) return rc;
+    if (rc) return bail(rc);
     *passes = 1;
     // second layer of two-layer chains: C = A (A B), the temporary is its B
     std::vector<BatchInput> in2;
@@ -177,19 +202,25 @@ int ServerImpl::issue(std::vector<std::shared_ptr<Request>>& take, int slot, uin
         }
     if (!in2.empty()) {
         rc = enqueue_pass(in2, take[0]->precision, stg + n, b->d_desc + n, b->d_counter, st);
-        if (rc) return rc;
+        if (rc) return bail(rc);
         *passes = 2;
     }
     for (auto& r : take) {
         e = cudaMemcpyAsync(r->C_host, r->dC, r->bytes_C, cudaMemcpyDeviceToHost, st);
-        if (e != cudaSuccess) ACC_FAIL(ACCSPMM_ERROR_CUDA, "result copy: %s", cudaGetErrorString(e));
-        cudaFreeAsync(r->dB, st);
-        cudaFreeAsync(r->dC, st);
-        if (r->dT) cudaFreeAsync(r->dT, st);
+        if (e != cudaSuccess) SERVER_FAIL(ACCSPMM_ERROR_CUDA, "result copy: %s", cudaGetErrorString(e));
+    }
+    for (auto& r : take) {
+        for (float** q : {&r->dB, &r->dC, &r->dT})
+            if (*q) {
+                cudaFreeAsync(*q, st);
+                *q = nullptr;
+            }
     }
     cudaFreeAsync(b->d_desc, st);
+    b->d_desc = nullptr;
     e = cudaLaunchHostFunc(st, &ServerImpl::on_done, b.get());
-    if (e != cudaSuccess) ACC_FAIL(ACCSPMM_ERROR_CUDA, "completion callback: %s", cudaGetErrorString(e));
+    if (e != cudaSuccess) SERVER_FAIL(ACCSPMM_ERROR_CUDA, "completion callback: %s", cudaGetErrorString(e));
+#undef SERVER_FAIL
     b.release();  // owned by the callback now
     return ACCSPMM_SUCCESS;
 }
