@@ -58,6 +58,22 @@ int copy_arr(T* dst, int32_t dspace, const T* src, int32_t sspace, size_t n, cud
 
 bool valid_space(int32_t s) { return s == ACCSPMM_HOST || s == ACCSPMM_DEVICE; }
 
+// A host CSR the host builders may index through: arrays present, row_ptr
+// from 0 to nnz without decreasing, columns below cols.
+int check_host_csr(const accspmm_csr_t* csr) {
+    if (csr->space != ACCSPMM_HOST) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "the CSR must be in host memory");
+    if (!csr->row_ptr || (csr->nnz && (!csr->col_idx || !csr->data)))
+        ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "CSR arrays missing");
+    if (csr->row_ptr[0] != 0) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "row_ptr[0] != 0");
+    if (csr->row_ptr[csr->rows] != csr->nnz) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "row_ptr[rows] != nnz");
+    for (uint32_t r = 0; r < csr->rows; ++r)
+        if (csr->row_ptr[r] > csr->row_ptr[r + 1])
+            ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "row_ptr decreases at row %u", r);
+    for (uint32_t i = 0; i < csr->nnz; ++i)
+        if (csr->col_idx[i] >= csr->cols) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "column %u >= cols", csr->col_idx[i]);
+    return ACCSPMM_SUCCESS;
+}
+
 }  // namespace
 
 extern "C" {
@@ -88,14 +104,7 @@ int accspmm_metcf_from_csr(const accspmm_csr_t* csr, accspmm_metcf_t* metcf, voi
     if (!csr->row_ptr || (csr->nnz && (!csr->col_idx || !csr->data)))
         ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "CSR arrays missing");
     if (csr->space == ACCSPMM_HOST) {
-        if (csr->row_ptr[csr->rows] != csr->nnz)
-            ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "row_ptr[rows] != nnz");
-        for (uint32_t r = 0; r < csr->rows; ++r)
-            if (csr->row_ptr[r] > csr->row_ptr[r + 1])
-                ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "row_ptr decreases at row %u", r);
-        for (uint32_t i = 0; i < csr->nnz; ++i)
-            if (csr->col_idx[i] >= csr->cols)
-                ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "column %u >= cols", csr->col_idx[i]);
+        if (int r = check_host_csr(csr)) return r;
         return metcf_from_csr_host(csr, metcf);
     }
     if (csr->space == ACCSPMM_DEVICE) return metcf_from_csr_device(csr, metcf, stream);
@@ -272,12 +281,14 @@ int accspmm_reorder_rcm(const accspmm_csr_t* csr, uint32_t* perm, uint64_t* band
                         uint64_t* bandwidth_after) {
     clear_error();
     if (!csr || !perm) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "null argument");
+    if (int r = check_host_csr(csr)) return r;
     return reorder_rcm_host(csr, perm, bandwidth_before, bandwidth_after);
 }
 
 int accspmm_csr_permute(const accspmm_csr_t* csr, const uint32_t* perm, accspmm_csr_t* out) {
     clear_error();
     if (!csr || !perm || !out) ACC_FAIL(ACCSPMM_ERROR_INVALID_VALUE, "null argument");
+    if (int r = check_host_csr(csr)) return r;
     return csr_permute_host(csr, perm, out);
 }
 

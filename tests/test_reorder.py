@@ -69,6 +69,31 @@ def test_bad_inputs_are_refused():
         api.csr_permute(csr, bad)
 
 
+@pytest.mark.parametrize("case", ["row_ptr_decreases", "last_offset_not_nnz", "first_offset_not_zero",
+                                  "column_past_cols"])
+def test_malformed_host_csr_is_refused_before_it_is_read(case):
+    """The host entry points that walk a CSR (RCM, P A P^T, the host METCF
+    builder) check its offsets and columns first and return
+    ACCSPMM_ERROR_INVALID_VALUE instead of reading past its arrays."""
+    csr, _ = shuffled_grid(side=10)
+    rp, ci = csr["row_ptr"].copy(), csr["col_idx"].copy()
+    if case == "row_ptr_decreases":
+        rp[5] = rp[7] + 1
+    elif case == "last_offset_not_nnz":
+        rp[-1] = csr["nnz"] + 8
+    elif case == "first_offset_not_zero":
+        rp[0] = 2
+    else:
+        ci[3] = csr["cols"] + 4
+    bad = dict(csr, row_ptr=rp, col_idx=ci)
+    perm = np.arange(csr["rows"], dtype=np.uint32)
+    for call in (lambda: api.reorder_rcm(bad), lambda: api.csr_permute(bad, perm),
+                 lambda: api.metcf_from_csr(bad)):
+        with pytest.raises(capi.AccSpmmError) as e:
+            call()
+        assert e.value.status == capi.ERROR_INVALID_VALUE
+
+
 @pytest.mark.gpu
 def test_reordered_product_maps_back_to_the_original():
     torch = pytest.importorskip("torch")
