@@ -48,11 +48,15 @@ struct DevBuf {
     cudaError_t alloc(size_t n, cudaStream_t st) {
         reset();
         s = st;
+        // a stream being captured into a graph allocates from the device's
+        // current pool, as before the library pool existed (creating that
+        // pool and its copy streams in the middle of a capture could end
+        // the capture); so does a call whose library pool cannot be created
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         cudaMemPool_t pool;
-        if (library_pool(&pool) == ACCSPMM_SUCCESS)
+        if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone &&
+            library_pool(&pool) == ACCSPMM_SUCCESS)
             return cudaMallocFromPoolAsync(reinterpret_cast<void**>(&p), sizeof(T) * (n ? n : 1), pool, st);
-        // no library pool (it could not be created here): the device's
-        // current pool
         return cudaMallocAsync(reinterpret_cast<void**>(&p), sizeof(T) * (n ? n : 1), st);
     }
     void reset() {
