@@ -130,3 +130,20 @@ def test_invalid_csr_rejected():
     with pytest.raises(capi.AccSpmmError) as e:
         api.metcf_from_csr(csr)
     assert e.value.status == capi.ERROR_INVALID_VALUE
+
+
+@pytest.mark.parametrize("params", [(3, 1, 2, 16), (2, 3, 5, 4), (1, 0, 0, 1), (10, 5, 7, 60), (7, 7, 7, 100)])
+def test_host_adpbme_groups_match_the_oracle(params):
+    """The host AdpBME packing equals the oracle's greedy walk for the
+    reference's parameters and for other cost settings (one-tile groups,
+    large targets)."""
+    rng = np.random.default_rng(sum(params))
+    rows, cols, nnz = 4000, 3000, 60000
+    r = np.sort(rng.integers(0, rows, nnz)).astype(np.uint32)
+    c = rng.integers(0, cols, nnz).astype(np.uint32)
+    v = rng.random(nnz, dtype=np.float32)
+    csr = api.csr_from_coo(rows, cols, r, c, v)
+    m = api.metcf_from_csr(csr)
+    a = api.adpbme_from_metcf(m, *params)
+    np.testing.assert_array_equal(a["group_offset"], oracle.adpbme_groups(m["rwo"], *params))
+    np.testing.assert_array_equal(a["row_indices"], oracle.adpbme_row_indices(m["rwo"]))
